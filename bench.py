@@ -1,0 +1,369 @@
+"""Benchmark: 512^2 AT reconstruction slices/s on one GB300 (BASELINE C2).
+
+Workload (C2): 512x512 FP32 slices, 0.75 mm pixels, fan beam (SOD 541 mm,
+SDD 949 mm) with 720 views x 888 equiangular detectors, seeded Shepp-Logan +
+20 random ellipses, Poisson noise at I0 = 5e3, 50 AT outer iterations with
+GoldenC's defaults (alpha 1000, beta 0.002, epsilon 1e-4, 10 image + 10 edge
+iterations each).  A step reconstructs a batch of slices from scratch
+(f = 0, v = 1) in one batched, graph-captured solver.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+value  : slices/s with the sinograms resident in HBM, CUDA-event timed over K
+         steps on the solver's stream, L2 flushed (256 MiB write) before every
+         step.
+e2e    : the same through the C-ABI with host buffers: every step copies the
+         sinograms in from pinned host memory and f, v back out.
+roofline: the dominant kernel timed alone with CUDA events on its stream, at
+         the same workload, against the measured HBM copy bandwidth.
+--impl reference: the reference algorithm on the host cores (the FP64 oracle
+         restatement of GoldenC's solver with the fan tracer, all threads), each
+         step one outer iteration of one slice, scaled to slices/s.
+N > 1 (torchrun): independent replicas, one per GPU ("replicas only").
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "512^2 AT recon slices/s"
+UNIT = "slices/s"
+WORKLOAD = ("C2 512x512 0.75mm fan-beam AT reconstruction: 720 views x 888 dets, SOD 541 / SDD 949 mm, "
+            "Shepp-Logan + 20 random ellipses, Poisson I0=5e3, 50 outer x (10 image CG + 10 edge) iterations")
+
+
+def env_rank():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[4:8]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profile_traffic(kernel: str):
+    """DRAM bytes per launch from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as fh:
+            return json.load(fh).get(kernel)
+    except (OSError, ValueError):
+        return None
+
+
+def make_inputs(mg, spec, batch: int):
+    """Seeded phantoms and noisy sinograms (projected by the engine itself)."""
+    plan = mg.Plan.fan(spec.geom)
+    phantoms, sinos = [], []
+    for b in range(batch):
+        ph = mg.phantom.ellipse_phantom(spec.geom.n, seed=spec.seed + b, n_random=spec.n_random)
+        clean = plan.forward(ph)
+        sinos.append(mg.phantom.poisson_sinogram(clean, spec.i0, spec.seed + 1000 + b))
+        phantoms.append(ph)
+    return plan, phantoms, sinos
+
+
+def run_ours(args):
+    import torch
+
+    import medimage_gb300 as mg
+    from medimage_gb300 import configs
+
+    rank, world, local = env_rank()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    spec = configs.c2()
+    B = args.batch
+    plan, phantoms, sinos = make_inputs(mg, spec, B)
+    S_seg = plan.stats["segments"]
+    R = plan.stats["rays"]
+    P = spec.geom.n * spec.geom.n
+    prm = configs.params_for(spec, mode=args.mode)
+    solver = mg.Solver([plan] * B, prm)
+    for b in range(B):
+        solver.set_sino(b, sinos[b])
+    import ctypes as C
+
+    stream_ptr = C.c_void_p()
+    mg.engine._check("at_stream_create", mg.lib().at_stream_create(C.byref(stream_ptr)))
+    st = stream_ptr.value
+    tstream = torch.cuda.ExternalStream(st)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def step():
+        with torch.cuda.stream(tstream):
+            flush.zero_()
+        solver.run(stream=st, sync=False)
+
+    for _ in range(args.warmup):
+        step()
+    solver.sync(st)
+    launches_outer = solver.launches_per_outer
+    # ---- value: device-resident inputs
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        ev0.record(tstream)
+        for _ in range(args.steps):
+            step()
+        ev1.record(tstream)
+        torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    slices = args.steps * B * world
+    value = slices / (ms / 1e3)
+    f0, v0 = solver.get(0, stream=st)
+    psnr = mg.phantom.psnr(f0, phantoms[0])
+    tr = solver.trace(0)
+
+    # ---- e2e: host buffers through the C-ABI, copies inside the timed region
+    pinned_in = [torch.empty(sinos[0].shape, dtype=torch.float32, pin_memory=True) for _ in range(B)]
+    for b in range(B):
+        pinned_in[b].numpy()[...] = sinos[b]
+    pin_f = [torch.empty((spec.geom.n, spec.geom.n), dtype=torch.float32, pin_memory=True) for _ in range(B)]
+    pin_v = [torch.empty((spec.geom.n, spec.geom.n), dtype=torch.float32, pin_memory=True) for _ in range(B)]
+    L = mg.lib()
+    fp32 = C.POINTER(C.c_float)
+
+    def e2e_step():
+        for b in range(B):
+            mg.engine._check("set_sino_host", L.at_solver_set_sino_host(
+                solver.handle, b, pinned_in[b].numpy(), C.c_void_p(st)))
+        solver.run(stream=st, sync=False)
+        for b in range(B):
+            mg.engine._check("get_host", L.at_solver_get_host(
+                solver.handle, b, pin_f[b].numpy(), pin_v[b].numpy(), C.c_void_p(st)))
+
+    e2e_step()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = slices / e2e_s
+    del fp32
+
+    # ---- roofline: the dominant kernel alone, same workload, CUDA events
+    d_img = torch.from_numpy(phantoms[0]).cuda()
+    d_sino = torch.from_numpy(sinos[0]).cuda()
+    d_out_s = torch.empty_like(d_sino)
+    d_out_i = torch.empty_like(d_img)
+    kern = {}
+    for name, fn, nbytes in (
+            ("fan_fp_kernel", lambda: plan.forward_dev(d_img.data_ptr(), d_out_s.data_ptr(), st), 4 * S_seg + 4 * R),
+            ("fan_bp_kernel", lambda: plan.back_dev(d_sino.data_ptr(), d_out_i.data_ptr(), st), 4 * S_seg + 4 * P)):
+        for _ in range(3):
+            fn()
+        reps = 20
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(tstream)
+        for _ in range(reps):
+            fn()
+        e1.record(tstream)
+        torch.cuda.synchronize()
+        kern[name] = {"ms": e0.elapsed_time(e1) / reps, "bytes": nbytes}
+    # calls per slice in the timed workload
+    K, KI = prm.iter_alt, prm.iter_image
+    fp_calls = K * (3 * KI - 1) if prm.mode == 0 else None
+    bp_calls = K * KI
+    if fp_calls is None:
+        fp_calls = K * (KI + 2)
+    share = {n: kern[n]["ms"] * (fp_calls if "fp" in n else bp_calls) for n in kern}
+    dom = max(share, key=share.get)
+    peak, peak_kind = measured_peak_hbm()
+    achieved = kern[dom]["bytes"] / (kern[dom]["ms"] / 1e3) / 1e9
+    traffic = profile_traffic(dom)
+    gsegs = S_seg * (fp_calls + bp_calls) * slices / (ms / 1e3) / 1e9
+    clocks = clk.summary()
+
+    out = None
+    if rank == 0:
+        cpu = cpu_baseline(spec, sinos[0], args.cpu_outer) if not args.no_cpu else None
+        out = {
+            "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded phantoms, Poisson noise)",
+            "config": {"workload": WORKLOAD, "slices_per_step": B, "mode": "exact" if prm.mode == 0 else "linear",
+                       "parallelism": f"replicas{world}", "l2": "flushed (256 MiB write) before every step",
+                       "segments_per_projection": S_seg, "projections_per_slice": {"forward": fp_calls, "back": bp_calls}},
+            "gsegs_per_s": round(gsegs, 3),
+            "psnr_db": round(psnr, 3),
+            "exits": [t[:4] for t in tr if t[3] != 0][:6],
+            "e2e": {"value": round(e2e_value, 4), "unit": UNIT, "h2d_bytes_per_step": int(B * sinos[0].nbytes),
+                    "d2h_bytes_per_step": int(B * 2 * phantoms[0].nbytes)},
+            "roofline": {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+                         "peak_source": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                         "traffic": traffic, "algorithmic_bytes_per_launch": kern[dom]["bytes"],
+                         "launch_ms": round(kern[dom]["ms"], 5),
+                         "kernels": {k: {"launch_ms": round(v["ms"], 5),
+                                         "achieved_gbs": round(v["bytes"] / (v["ms"] / 1e3) / 1e9, 1)}
+                                     for k, v in kern.items()}},
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+            "gpu_launches": int(args.steps * (1 + prm.iter_alt * launches_outer)),
+        }
+        print(json.dumps(out))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return out
+
+
+def cpu_baseline(spec, sino, outer: int):
+    """The FP64 oracle (reference algorithm) on all host cores: `outer` outer
+    iterations of one slice, scaled to slices/s."""
+    from oracle import pyoracle as po
+
+    cores = os.cpu_count() or 1
+    fan = po.fan_from_engine(spec.geom)
+    t0 = time.perf_counter()
+    po.solve(fan, sino.astype(np.float64), 1000.0, 0.002, 1e-4, outer, 10, 10, nthreads=cores)
+    dt = time.perf_counter() - t0
+    per_slice = dt / outer * spec.iters
+    return {"value": round(1.0 / per_slice, 6), "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{outer} of {spec.iters} outer iterations of one C2 slice (FP64 oracle restatement of "
+                      f"GoldenC main.c with the helical/rebin fan tracer, OpenMP {cores} threads), "
+                      f"{dt:.2f} s, scaled x{spec.iters / outer:g}"}
+
+
+def run_reference(args):
+    """--impl reference: the reference algorithm on the host cores."""
+    rank, world, _ = env_rank()
+    if rank != 0:
+        return None
+    import medimage_gb300.configs as configs
+    from medimage_gb300.phantom import ellipse_phantom, poisson_sinogram
+    from oracle import pyoracle as po
+
+    spec = configs.c2()
+    fan = po.fan_from_engine(spec.geom)
+    cores = os.cpu_count() or 1
+    ph = ellipse_phantom(spec.geom.n, seed=spec.seed, n_random=spec.n_random)
+    clean = po.fan_A(fan, ph.astype(np.float64), cores)
+    sino = poisson_sinogram(clean, spec.i0, spec.seed + 1000).astype(np.float64)
+    for _ in range(args.warmup and 1):
+        po.solve(fan, sino, 1000.0, 0.002, 1e-4, 1, 10, 10, nthreads=cores)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        po.solve(fan, sino, 1000.0, 0.002, 1e-4, 1, 10, 10, nthreads=cores)
+    dt = time.perf_counter() - t0
+    per_outer = dt / args.steps
+    value = 1.0 / (per_outer * spec.iters)
+    out = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 6), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(per_outer * 1e3, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded phantoms, Poisson noise)",
+        "config": {"workload": WORKLOAD, "slices_per_step": 1, "sample": "one outer iteration per step"},
+        "cpu_baseline": {"value": round(value, 6), "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": "each step = 1 of 50 outer iterations of one C2 slice, FP64 oracle restatement "
+                                   "of GoldenC main.c + helical/rebin fan tracer, OpenMP; scaled x50"},
+        "e2e": {"value": round(value, 6), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--batch", type=int, default=4, help="slices reconstructed together per step")
+    ap.add_argument("--mode", type=int, default=0, help="0 exact projection count, 1 linear-mode updates")
+    ap.add_argument("--cpu-outer", type=int, default=1, help="outer iterations in the CPU baseline sample")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

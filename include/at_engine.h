@@ -1,0 +1,160 @@
+/*
+ * at_engine.h -- native C-ABI of the GB300 Ambrosio-Tortorelli CT engine.
+ *
+ * Plain C types only: pointers, sizes and status codes.  Every call returns 0
+ * on success or a negative AT_E* code; at_last_error() then holds a message.
+ * Pointers named d_* are device (HBM) pointers; h_* are host pointers.
+ * `stream` is a cudaStream_t passed as void* (NULL = the legacy default stream).
+ *
+ * Reference interfaces these entry points replace (paths relative to the
+ * reference project root):
+ *   at_forward / at_forward_host      A(proj, orig)             origin/GoldenC/src/proj.c:14-204
+ *                                     fan-beam forward_proj     helical/rebin/src/tracing.cpp:22-147
+ *   at_back / at_back_host            AStar(back, proj)         origin/GoldenC/src/proj.c:206-397
+ *   at_solver_run / at_reconstruct_*  MumfordShah(alpha,beta,eps) origin/GoldenC/src/main.c:35-49
+ *                                     with minimize_in_IMAGE_variable main.c:81-257 and
+ *                                     minimize_in_EDGE_variable main.c:259-360
+ *   at_fan_geometry                   NX NY vx vy NDETECTOR NPROJ SOURCE_TO_ISO SOURCE_TO_DET
+ *                                     LENGTH_PER_DET OFF_CENTER  helical/rebin/src/main.h:16-47
+ *   at_params                         ALPHA BETA EPSILON _IterAlt _IterImage _IterEdge
+ *                                     origin/GoldenC/src/config.h:6-17
+ * The GoldenC link-level symbols themselves (A, AStar, ...) are declared in
+ * goldnc.h and exported by the same library.
+ */
+#ifndef AT_ENGINE_H
+#define AT_ENGINE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define AT_OK 0
+#define AT_EINVAL (-1)   /* bad argument or geometry                    */
+#define AT_ECUDA (-2)    /* CUDA runtime error                          */
+#define AT_ENOMEM (-3)   /* device or host allocation failed            */
+#define AT_ESTATE (-4)   /* call not valid in the object's current state */
+#define AT_EBUDGET (-5)  /* request does not fit the admission budget   */
+#define AT_ETIMEOUT (-6) /* a bounded device wait gave up               */
+
+/* geometry kinds */
+#define AT_GEOM_GOLDNC 0 /* GoldenC parallel beam: 512x512, 180 views x 767 detectors */
+#define AT_GEOM_FAN 1    /* 2D fan beam with an equiangular detector                */
+
+/* 2D fan-beam geometry, the parameters of helical/rebin (main.h:16-47,
+ * ms2d.cpp:30-62,172-183).  Image n x n, pixel index x*n + y (x slow),
+ * image spans [0, n*pixel_mm]^2; source of view k at angle
+ * view0_deg + k*view_step_deg around the image centre at sod_mm; detector j
+ * (j = -ndets/2 .. ndets/2-1) at angle (j + off_center)*det_pitch_deg + 180
+ * degrees from the source, sdd_mm away.  ndets must be even. */
+typedef struct at_fan_geometry {
+    int32_t n;
+    double pixel_mm;
+    int32_t nviews;
+    int32_t ndets;
+    double sod_mm;
+    double sdd_mm;
+    double det_pitch_deg;
+    double off_center;
+    double view0_deg;
+    double view_step_deg;
+} at_fan_geometry;
+
+/* AT functional weights and iteration counts (config.h:6-8,15-17).
+ * mode 0 ("exact") makes every projection the reference makes (29 forward and
+ * 10 back projections per outer iteration at iter_image = 10).  mode 1
+ * ("linear") replaces the forward projections that linearity of A makes
+ * redundant (A(p_new) = A(d) + c2 A(p_old), A(f + c1 p) = A f + c1 A p when no
+ * median step intervened) by sinogram updates. */
+typedef struct at_params {
+    double alpha;
+    double beta;
+    double epsilon;
+    int32_t iter_alt;
+    int32_t iter_image; /* >= 2 (the reference divides by iter_image/2) */
+    int32_t iter_edge;
+    int32_t mode;
+} at_params;
+
+typedef struct at_plan at_plan;     /* device-resident projector plan of one geometry */
+typedef struct at_solver at_solver; /* device-resident state of a batch of scans      */
+
+typedef struct at_plan_stats {
+    int32_t kind;
+    int32_t n, nviews, ndets;
+    int64_t rays;          /* rays traced                                      */
+    int64_t segments;      /* S: ray-pixel segments summed over all rays        */
+    int64_t offgrid;       /* segments the reference traces off the pixel grid */
+    int64_t device_bytes;  /* plan memory in HBM                               */
+    int32_t max_segments;  /* longest ray                                      */
+} at_plan_stats;
+
+const char *at_last_error(void);
+int at_device_info(char *name, int name_len, int *sm_count, size_t *hbm_bytes);
+
+/* ---- plans ---- */
+int at_plan_create_fan(const at_fan_geometry *geom, at_plan **out);
+int at_plan_create_goldnc(at_plan **out);
+void at_plan_destroy(at_plan *plan);
+int at_plan_get_stats(const at_plan *plan, at_plan_stats *out);
+/* Traversal of one ray as the device plan stores it: pixel indices and FP32
+ * weights in visiting order.  For AT_GEOM_GOLDNC, (view, det) address the
+ * traced walk (alpha = view 1..45, raynum = det 0..383) and pixel indices are
+ * row*512+col of the tile-global walk (symmetry 0), all 16 tiles in order. */
+int at_plan_trace_ray(const at_plan *plan, int32_t view, int32_t det, int32_t *h_pix, float *h_w,
+                      int32_t cap, int32_t *n_out);
+
+/* ---- projectors (FP32, device buffers) ---- */
+/* d_sino[view][det] = sum over the ray's segments of d_img[pixel] * weight */
+int at_forward(const at_plan *plan, const float *d_img, float *d_sino, void *stream);
+/* d_img = A^T d_sino, a deterministic per-pixel gather (no atomics) */
+int at_back(const at_plan *plan, const float *d_sino, float *d_img, void *stream);
+/* host-buffer forms: copy in, project, copy out, synchronise */
+int at_forward_host(const at_plan *plan, const float *h_img, float *h_sino);
+int at_back_host(const at_plan *plan, const float *h_sino, float *h_img);
+
+/* ---- device memory helpers for callers without a CUDA runtime binding ---- */
+int at_dev_alloc(void **d_ptr, size_t bytes);
+int at_dev_free(void *d_ptr);
+int at_memcpy_h2d(void *d_dst, const void *h_src, size_t bytes, void *stream);
+int at_memcpy_d2h(void *h_dst, const void *d_src, size_t bytes, void *stream);
+int at_stream_create(void **stream);
+int at_stream_destroy(void *stream);
+int at_stream_sync(void *stream);
+
+/* ---- AT solver over a batch of scans ----
+ * Every scan has its own plan (geometry), sinogram, f, v and CG state; all
+ * scans advance together, one launch per kernel for the whole batch, and each
+ * decides its own early exits on the device.  One outer iteration (image step
+ * + edge step) is captured once as a CUDA graph and replayed. */
+int at_solver_create(at_plan *const *plans, int32_t nscans, const at_params *params, at_solver **out);
+void at_solver_destroy(at_solver *s);
+/* Device bytes the solver would hold for these plans (admission control). */
+int at_solver_footprint(at_plan *const *plans, int32_t nscans, size_t *bytes);
+int at_solver_set_sino(at_solver *s, int32_t scan, const float *d_sino, void *stream);
+int at_solver_set_sino_host(at_solver *s, int32_t scan, const float *h_sino, void *stream);
+/* f = 0, v = 1 for all scans (main.c:36-40); called by at_solver_run. */
+int at_solver_reset(at_solver *s, void *stream);
+/* Runs params.iter_alt outer iterations on `stream` (asynchronous). */
+int at_solver_run(at_solver *s, void *stream);
+/* Runs `count` outer iterations without resetting (for interleaving). */
+int at_solver_step(at_solver *s, int32_t count, void *stream);
+int at_solver_get(at_solver *s, int32_t scan, float *d_f, float *d_v, void *stream);
+int at_solver_get_host(at_solver *s, int32_t scan, float *h_f, float *h_v, void *stream);
+/* Scalar trajectory of one scan: records of {outer, step, k, exit, s[6]} as
+ * doubles (10 per record), the scalars the reference prints (main.c:251,330). */
+int at_solver_trace(at_solver *s, int32_t scan, double *h_recs, int32_t cap, int32_t *n_out);
+/* Kernel launches one outer iteration makes (graph node count). */
+int at_solver_launches_per_outer(const at_solver *s, int32_t *n);
+
+/* One call, host buffers: sinogram in, f and v out (H2D, solve, D2H). */
+int at_reconstruct_host(const at_plan *plan, const at_params *params, const float *h_sino, float *h_f,
+                        float *h_v);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,35 @@
+"""medimage_gb300 -- GB300-native Ambrosio-Tortorelli CT reconstruction engine.
+
+Python host bindings over the C-ABI of ``include/at_engine.h`` and the GoldenC
+drop-in symbols of ``include/goldnc.h``, both exported by the in-tree
+``medimage_gb300/libat_engine.so`` (built by ``medimage_gb300/build.py``).
+
+There is no CPU fallback: every call goes to the CUDA library, and importing
+the bindings raises if the library is missing.
+"""
+from __future__ import annotations
+
+from .engine import (  # noqa: F401
+    AtError,
+    FanGeometry,
+    Params,
+    Plan,
+    Solver,
+    device_info,
+    lib,
+    reconstruct,
+)
+from . import configs, phantom  # noqa: F401
+
+__all__ = [
+    "AtError",
+    "FanGeometry",
+    "Params",
+    "Plan",
+    "Solver",
+    "configs",
+    "device_info",
+    "lib",
+    "phantom",
+    "reconstruct",
+]

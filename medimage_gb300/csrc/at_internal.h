@@ -1,0 +1,95 @@
+// at_internal.h -- types shared by the engine's translation units.
+//
+// Layout of a fan-beam plan in HBM (one per geometry, built once on the GPU):
+//   rays   : RayHdr[nviews*ndets]      32 B per ray (start pixel, segment count,
+//                                        FP32 boundary parameters)
+//   bits   : uint32 decision words      1 bit per Siddon segment (1 = the ray
+//                                        crosses an x plane, 0 = a y plane),
+//                                        block-interleaved: block b (128 rays of
+//                                        one view) stores word w of ray i at
+//                                        bits[blk_word[b] + w*128 + i]
+//   blk_word: uint32[nblocks+1]         word offset of each 128-ray block
+//   blk_nw  : uint8 [nblocks]           decision words of the block's longest ray
+// GoldenC plan: traced walks of proj.c as explicit FP32 segments (CSR by
+// (alpha, raynum) pair) plus the transposed list (CSC by pixel) for the gather.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+
+#include <cuda_runtime.h>
+
+#include "../../include/at_engine.h"
+
+namespace at {
+
+constexpr int kRayBlock = 128;  // rays per decision-bit block (one view)
+
+// Per-ray header.  Boundary parameters are relative to the ray's entry
+// lambda_min (mm): the k-th x-plane crossing is at fmaf(k, lenx, ax), the k-th
+// y-plane crossing at fmaf(k, leny, ay); a segment's weight is the difference
+// of consecutive crossings.
+struct __align__(16) RayHdr {
+  int32_t pix0;   // x0*n + y0 of the first pixel
+  int32_t nseg;   // segments the reference's loop emits
+  int32_t xy0;    // x0 | (y0 << 16)
+  int32_t sgn;    // bit0: signx > 0, bit1: signy > 0
+  float ax, ay, lenx, leny;
+};
+static_assert(sizeof(RayHdr) == 32, "RayHdr must stay 32 bytes");
+
+struct GcSeg {   // one GoldenC walk segment
+  int32_t pix;   // Y*512 + X (tile-global, symmetry 0 frame)
+  float w;
+};
+struct GcEntry { // transposed entry at a symmetry-0 pixel
+  int32_t pair;  // (alpha-1)*384 + raynum
+  float w;
+};
+
+struct Plan {
+  int kind = AT_GEOM_FAN;
+  at_fan_geometry geom{};
+  int n = 0, nviews = 0, ndets = 0;
+  int64_t rays = 0, segments = 0, offgrid = 0, device_bytes = 0;
+  int max_segments = 0;
+  // fan
+  RayHdr *rays_d = nullptr;
+  uint32_t *bits_d = nullptr;
+  uint32_t *blk_word_d = nullptr;
+  uint8_t *blk_nw_d = nullptr;
+  int nblocks_per_view = 0, nblocks = 0;
+  float4 *view_d = nullptr;  // per view: {sx, sy, cos(beta), sin(beta)} (mm, FP32)
+  float det_inv_pitch = 0.f; // 1/detector pitch (rad^-1)
+  float det_t0 = 0.f;        // ndets/2 - off_center
+  // goldnc
+  GcSeg *gc_seg_d = nullptr;
+  int32_t *gc_pair_off_d = nullptr;  // [17280+1]
+  GcEntry *gc_ent_d = nullptr;
+  int32_t *gc_pix_off_d = nullptr;   // [512*512+1]
+  ~Plan();
+};
+
+// error state (thread-local message + status)
+int set_error(int code, const std::string &msg);
+int cuda_error(cudaError_t e, const char *what);
+#define AT_CUDA_TRY(expr)                                   \
+  do {                                                      \
+    cudaError_t _e = (expr);                                \
+    if (_e != cudaSuccess) return ::at::cuda_error(_e, #expr); \
+  } while (0)
+
+// host-side geometry tables with the reference's libm expressions
+void fan_tables(const at_fan_geometry &g, double *scos, double *ssin, double *dcos, double *dsin);
+int validate_fan(const at_fan_geometry &g);
+
+// plan construction (plan.cu)
+int build_fan_plan(Plan &p, cudaStream_t st);
+int build_goldnc_plan(Plan &p, cudaStream_t st);
+
+}  // namespace at
+
+struct at_plan {
+  at::Plan p;
+};

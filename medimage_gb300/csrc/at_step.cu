@@ -1,0 +1,309 @@
+// at_step.cu -- pixel and sinogram passes of the AT iteration
+// (origin/GoldenC/src/main.c:81-390) for a batch of scans.
+//
+// Pixel passes use 8 x 32 tiles (x rows, y columns; 256 threads), the same
+// CTA numbering as the back projector, so one prefix table serves both.  Each
+// pass fuses the elementwise update with the reductions the next scalar step
+// needs; neighbours of freshly computed values are recomputed from their
+// inputs instead of being re-read, so no pass waits on another one.
+#include <cuda_runtime.h>
+
+#include "solver_dev.cuh"
+
+namespace at {
+
+struct PixCoord {
+  int x, y, i;
+  bool inside;
+};
+
+__device__ __forceinline__ PixCoord pix_of(int n, int local_cta) {
+  const int tiles_y = (n + 31) >> 5;
+  PixCoord c;
+  c.x = (local_cta / tiles_y) * 8 + (threadIdx.x >> 5);
+  c.y = (local_cta % tiles_y) * 32 + (threadIdx.x & 31);
+  c.inside = c.x < n && c.y < n;
+  c.i = c.x * n + c.y;
+  return c;
+}
+
+#define AT_SCAN_PROLOGUE                                                              \
+  const int scan = find_scan(L.prefix, L.nscans, blockIdx.x);                         \
+  const ScanDev &S = L.scans[scan];                                                   \
+  if (!flow_active(S, L.flow)) return;                                                \
+  const int cta0 = __ldg(L.prefix + scan);                                            \
+  const int ncta = __ldg(L.prefix + scan + 1) - cta0;                                 \
+  const int local_cta = blockIdx.x - cta0;                                            \
+  (void)ncta;
+
+__device__ __forceinline__ float warp_max_f(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+__device__ __forceinline__ void sort2(float &a, float &b) {
+  const float lo = fminf(a, b), hi = fmaxf(a, b);
+  a = lo;
+  b = hi;
+}
+__device__ __forceinline__ float med3(float a, float b, float c) {
+  return fmaxf(fminf(a, b), fminf(fmaxf(a, b), c));
+}
+
+// Median of a 3x3 window: sort each row, then the median of nine is the median
+// of (largest row minimum, median of row medians, smallest row maximum).
+__device__ __forceinline__ float median9(float r0[3], float r1[3], float r2[3]) {
+  float *rows[3] = {r0, r1, r2};
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    float *r = rows[k];
+    sort2(r[0], r[1]);
+    sort2(r[1], r[2]);
+    sort2(r[0], r[1]);
+  }
+  const float a = fmaxf(fmaxf(r0[0], r1[0]), r2[0]);
+  const float b = med3(r0[1], r1[1], r2[1]);
+  const float c = fminf(fminf(r0[2], r1[2]), r2[2]);
+  return med3(a, b, c);
+}
+
+// update_next = update_cur + c1 p, 3x3 median (zero padding) when flag is set;
+// maxCP = max |c1 p|.  main.c:169-191, 366-390.
+__global__ void __launch_bounds__(256) upd_kernel(const Launch L) {
+  AT_SCAN_PROLOGUE
+  const int n = S.n;
+  const PixCoord c = pix_of(n, local_cta);
+  const float *__restrict__ u = S.buf[L.aux_buf];
+  const float *__restrict__ p = S.buf[L.in_buf];
+  float *__restrict__ out = S.buf[L.out_buf];
+  const float c1 = (float)S.ctl->c1;
+  float cp = 0.f;
+  if (c.inside) {
+    const float pc = p[c.i];
+    cp = fabsf(c1 * pc);
+    if (!L.flag) {
+      out[c.i] = fmaf(c1, pc, u[c.i]);
+    } else {
+      float w[3][3];
+#pragma unroll
+      for (int dx = -1; dx <= 1; dx++)
+#pragma unroll
+        for (int dy = -1; dy <= 1; dy++) {
+          const int xx = c.x + dx, yy = c.y + dy;
+          float val = 0.f;
+          if (xx >= 0 && xx < n && yy >= 0 && yy < n) {
+            const int j = xx * n + yy;
+            val = fmaf(c1, p[j], u[j]);
+          }
+          w[dx + 1][dy + 1] = val;
+        }
+      out[c.i] = median9(w[0], w[1], w[2]);
+    }
+  }
+  cp = warp_max_f(cp);
+  if ((threadIdx.x & 31) == 0 && cp > 0.f) atomic_max_nonneg(&S.ctl->maxbits, cp);
+  reduce_and_finalize<0>(S, L, nullptr, local_cta, ncta);
+}
+
+// p_new = d + c2 p_old (p_new = d on the first pass), nV = sum over all pixels
+// (v^2 + 0.01 eps^2) |backward grad p_new|^2 (p zero-padded), pd = <p_new, d>.
+// main.c:141-162, 247-250.
+__global__ void __launch_bounds__(256) pp_kernel(const Launch L) {
+  AT_SCAN_PROLOGUE
+  const int n = S.n;
+  const PixCoord c = pix_of(n, local_cta);
+  const float *__restrict__ d = S.buf[B_D];
+  const float *__restrict__ po = S.buf[L.in_buf];
+  const float *__restrict__ v = S.buf[B_V];
+  float *__restrict__ pn = S.buf[L.out_buf];
+  const bool first = L.flag != 0;
+  const float c2 = first ? 0.f : (float)S.ctl->c2;
+  double sums[2] = {0.0, 0.0};
+  if (c.inside) {
+    auto pnew = [&](int j) -> float { return first ? d[j] : fmaf(c2, po[j], d[j]); };
+    const float dc = d[c.i];
+    const float pc = pnew(c.i);
+    pn[c.i] = pc;
+    const float pu = c.x > 0 ? pnew(c.i - n) : 0.f;
+    const float pl = c.y > 0 ? pnew(c.i - 1) : 0.f;
+    const double vv = (double)v[c.i];
+    const double eps = S.ctl->eps;
+    const double a = (double)pc - pu, b = (double)pc - pl;
+    sums[0] = (vv * vv + 0.01 * eps * eps) * (a * a + b * b);
+    sums[1] = (double)pc * (double)dc;
+  }
+  reduce_and_finalize<2>(S, L, sums, local_cta, ncta);
+}
+
+// F = U1 when the image step ended in update buffer 1.
+__global__ void __launch_bounds__(256) commit_kernel(const Launch L) {
+  AT_SCAN_PROLOGUE
+  const PixCoord c = pix_of(S.n, local_cta);
+  if (c.inside && S.ctl->final_u == 1) S.buf[B_F][c.i] = S.buf[B_U1][c.i];
+}
+
+// |grad f|^2 with central differences, f zero-padded (main.c:296-298).
+__global__ void __launch_bounds__(256) edge_init_kernel(const Launch L) {
+  AT_SCAN_PROLOGUE
+  const int n = S.n;
+  const PixCoord c = pix_of(n, local_cta);
+  if (!c.inside) return;
+  const float *__restrict__ f = S.buf[B_F];
+  const float fd = c.x + 1 < n ? f[c.i + n] : 0.f, fu = c.x > 0 ? f[c.i - n] : 0.f;
+  const float fr = c.y + 1 < n ? f[c.i + 1] : 0.f, fl = c.y > 0 ? f[c.i - 1] : 0.f;
+  const float gx = 0.5f * (fd - fu), gy = 0.5f * (fr - fl);
+  S.buf[B_NN][c.i] = gx * gx + gy * gy;
+}
+
+// d = -(alpha v n - beta eps lap/4 v + beta (v-1)/(4 eps)), v one-padded
+// (main.c:299-309); sums nD, sum n d^2, nNablaD (d zero-padded, main.c:314-328).
+__global__ void __launch_bounds__(256) edge_d_kernel(const Launch L) {
+  AT_SCAN_PROLOGUE
+  const int n = S.n;
+  const PixCoord c = pix_of(n, local_cta);
+  const float *__restrict__ v = S.buf[B_V];
+  const float *__restrict__ nn = S.buf[B_NN];
+  const Ctl *ct = S.ctl;
+  const float alpha = (float)ct->alpha, beq = (float)(ct->beta * ct->eps);
+  const float b4 = (float)(ct->beta / (4 * ct->eps));
+  double sums[3] = {0.0, 0.0, 0.0};
+  if (c.inside) {
+    auto vat = [&](int xx, int yy) -> float {
+      return (xx >= 0 && xx < n && yy >= 0 && yy < n) ? v[xx * n + yy] : 1.f;
+    };
+    auto dat = [&](int xx, int yy) -> float {
+      if (xx < 0 || xx >= n || yy < 0 || yy >= n) return 0.f;
+      const float vc = v[xx * n + yy];
+      const float lap = 0.25f * (vat(xx + 1, yy) + vat(xx, yy + 1) - 4.f * vc + vat(xx - 1, yy) + vat(xx, yy - 1));
+      const float g = alpha * vc * nn[xx * n + yy] - beq * lap + b4 * (vc - 1.f);
+      return -g;
+    };
+    const float dc = dat(c.x, c.y);
+    S.buf[B_D][c.i] = dc;
+    const double dd = (double)dc * dc;
+    sums[0] = dd;
+    sums[1] = (double)nn[c.i] * dd;
+    const double gx = 0.5 * ((double)dat(c.x + 1, c.y) - (double)dat(c.x - 1, c.y));
+    const double gy = 0.5 * ((double)dat(c.x, c.y + 1) - (double)dat(c.x, c.y - 1));
+    sums[2] = gx * gx + gy * gy;
+  }
+  reduce_and_finalize<3>(S, L, sums, local_cta, ncta);
+}
+
+// v = clamp(v + c d, 0, 1); maxCD = max |c d| (main.c:332-344).
+__global__ void __launch_bounds__(256) edge_upd_kernel(const Launch L) {
+  AT_SCAN_PROLOGUE
+  const PixCoord c = pix_of(S.n, local_cta);
+  const float cc = (float)S.ctl->c;
+  float cd = 0.f;
+  if (c.inside) {
+    float *v = S.buf[B_V];
+    const float step = cc * S.buf[B_D][c.i];
+    cd = fabsf(step);
+    v[c.i] = fminf(fmaxf(v[c.i] + step, 0.f), 1.f);
+  }
+  cd = warp_max_f(cd);
+  if ((threadIdx.x & 31) == 0 && cd > 0.f) atomic_max_nonneg(&S.ctl->maxbits, cd);
+  reduce_and_finalize<0>(S, L, nullptr, local_cta, ncta);
+}
+
+// linear mode: q = Ad + c2 q with |q|^2 (ST_SQ) or Af += c1 q, r -= c1 q with
+// E_data (ST_SA).  256 bins per CTA.
+__global__ void __launch_bounds__(256) sino_kernel(const Launch L) {
+  AT_SCAN_PROLOGUE
+  const int b = local_cta * 256 + threadIdx.x;
+  double s[1] = {0.0};
+  if (b < S.nbins) {
+    float *q = S.buf[B_Q];
+    if (L.stage == ST_SQ) {
+      const float qn = fmaf((float)S.ctl->c2, q[b], S.buf[B_AD][b]);
+      q[b] = qn;
+      s[0] = (double)qn * qn;
+    } else {
+      const float c1 = (float)S.ctl->c1;
+      const float qb = q[b];
+      const float af = fmaf(c1, qb, S.buf[B_AF][b]);
+      S.buf[B_AF][b] = af;
+      S.buf[B_R][b] = S.buf[B_R][b] - c1 * qb;
+      const double dv = (double)af - (double)S.buf[B_G][b];
+      s[0] = dv * dv;
+    }
+  }
+  reduce_and_finalize<1>(S, L, s, local_cta, ncta);
+}
+
+// f = 0, v = 1 (main.c:36-40).
+__global__ void __launch_bounds__(256) init_state_kernel(const Launch L) {
+  AT_SCAN_PROLOGUE
+  const PixCoord c = pix_of(S.n, local_cta);
+  if (!c.inside) return;
+  S.buf[B_F][c.i] = 0.f;
+  S.buf[B_V][c.i] = 1.f;
+}
+
+// step boundaries: flag 0 = begin image step, 1 = begin edge step.
+__global__ void flags_kernel(const ScanDev *scans, int nscans, int mode) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nscans) return;
+  Ctl *c = scans[s].ctl;
+  if (!c->enabled) return;
+  c->arrive = 0u;
+  c->maxbits = 0u;
+  c->k = 1;
+  if (mode == 0) {
+    c->outer += 1;
+    c->img_active = 1;
+    c->final_u = 0;
+  } else {
+    c->edge_active = 1;
+  }
+}
+
+cudaError_t launch_pixel(int which, const Launch &L, int nctas, cudaStream_t st) {
+  switch (which) {
+    case 0: upd_kernel<<<nctas, 256, 0, st>>>(L); break;
+    case 1: pp_kernel<<<nctas, 256, 0, st>>>(L); break;
+    case 2: commit_kernel<<<nctas, 256, 0, st>>>(L); break;
+    case 3: edge_init_kernel<<<nctas, 256, 0, st>>>(L); break;
+    case 4: edge_d_kernel<<<nctas, 256, 0, st>>>(L); break;
+    case 5: edge_upd_kernel<<<nctas, 256, 0, st>>>(L); break;
+    case 6: sino_kernel<<<nctas, 256, 0, st>>>(L); break;
+    case 7: init_state_kernel<<<nctas, 256, 0, st>>>(L); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_flags(const ScanDev *scans, int nscans, int mode, cudaStream_t st) {
+  flags_kernel<<<(nscans + 63) / 64, 64, 0, st>>>(scans, nscans, mode);
+  return cudaGetLastError();
+}
+
+}  // namespace at
+
+namespace at {
+
+// Standalone 3x3 median with zero padding (main.c:366-390), out of place.
+__global__ void __launch_bounds__(256) median_kernel(const float *__restrict__ in, float *__restrict__ out, int n) {
+  const int y = blockIdx.x * 32 + (threadIdx.x & 31);
+  const int x = blockIdx.y * 8 + (threadIdx.x >> 5);
+  if (x >= n || y >= n) return;
+  float w[3][3];
+#pragma unroll
+  for (int dx = -1; dx <= 1; dx++)
+#pragma unroll
+    for (int dy = -1; dy <= 1; dy++) {
+      const int xx = x + dx, yy = y + dy;
+      w[dx + 1][dy + 1] = (xx >= 0 && xx < n && yy >= 0 && yy < n) ? in[xx * n + yy] : 0.f;
+    }
+  out[x * n + y] = median9(w[0], w[1], w[2]);
+}
+
+cudaError_t launch_median(const float *in, float *out, int n, cudaStream_t st) {
+  dim3 grid((n + 31) / 32, (n + 7) / 8);
+  median_kernel<<<grid, 256, 0, st>>>(in, out, n);
+  return cudaGetLastError();
+}
+
+}  // namespace at

@@ -1,0 +1,45 @@
+// geometry.cpp -- host-side geometry tables and validation.
+//
+// Built with -ffp-contract=off so the trig arguments are rounded exactly as in
+// the reference (x86-64 and aarch64 alike); the FP64 traversal on the GPU
+// starts from these values.
+#include <cmath>
+#include <string>
+
+#include "at_internal.h"
+
+namespace at {
+
+// helical/rebin/src/ms2d.cpp:43-54: source angle table (degrees -> cos/sin)
+// and the equiangular detector table with OFF_CENTER.
+void fan_tables(const at_fan_geometry &g, double *scos, double *ssin, double *dcos, double *dsin) {
+  for (int v = 0; v < g.nviews; v++) {
+    const double angle = g.view0_deg + v * g.view_step_deg;
+    scos[v] = std::cos(angle / 180.0 * M_PI);
+    ssin[v] = std::sin(angle / 180.0 * M_PI);
+  }
+  const double per_rad = g.det_pitch_deg * M_PI / 180.;
+  const int half = g.ndets / 2;
+  for (int j = -half; j < half; ++j) {
+    dcos[j + half] = std::cos((j + g.off_center) * per_rad + M_PI);
+    dsin[j + half] = std::sin((j + g.off_center) * per_rad + M_PI);
+  }
+}
+
+int validate_fan(const at_fan_geometry &g) {
+  if (g.n < 8 || g.n > 16384) return set_error(AT_EINVAL, "fan geometry: n must be in [8, 16384]");
+  if (g.nviews < 1 || g.nviews > 65536) return set_error(AT_EINVAL, "fan geometry: nviews must be in [1, 65536]");
+  if (g.ndets < 2 || g.ndets > 65536 || (g.ndets & 1))
+    return set_error(AT_EINVAL, "fan geometry: ndets must be even and in [2, 65536]");
+  if (!(g.pixel_mm > 0) || !(g.sdd_mm > g.sod_mm) || !(g.det_pitch_deg > 0))
+    return set_error(AT_EINVAL, "fan geometry: need pixel_mm > 0, sdd_mm > sod_mm, det_pitch_deg > 0");
+  const double r = g.n * g.pixel_mm * std::sqrt(2.0) / 2.0;
+  if (!(g.sod_mm > r * 1.0001))
+    return set_error(AT_EINVAL, "fan geometry: the source circle must lie outside the image");
+  const double half_fan_rad = (g.ndets / 2 + std::fabs(g.off_center)) * g.det_pitch_deg * M_PI / 180.0;
+  if (half_fan_rad >= M_PI / 2) return set_error(AT_EINVAL, "fan geometry: fan angle must stay below 180 degrees");
+  if ((int64_t)g.nviews * g.ndets > (1ll << 31) / 2) return set_error(AT_EINVAL, "fan geometry: too many rays");
+  return AT_OK;
+}
+
+}  // namespace at

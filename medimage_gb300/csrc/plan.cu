@@ -1,0 +1,483 @@
+// plan.cu -- one-time projector plans, built on the GPU in FP64.
+//
+// Compiled with --fmad=false: every FP64 expression below is evaluated as
+// separately rounded IEEE operations in the reference's order, so the traced
+// pixel sequences are bit-identical to the reference's CPU traversal.  Trig
+// tables come from the host's libm (see geometry.cpp), as in the reference.
+//
+// Fan beam  : helical/rebin/src/tracing.cpp:22-147 on the end points of
+//             helical/rebin/src/ms2d.cpp:172-183.
+// GoldenC   : origin/GoldenC/src/proj.c:38-200 (tile walks).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "at_internal.h"
+
+namespace at {
+
+// ---------------------------------------------------------------------------
+// fan beam
+// ---------------------------------------------------------------------------
+struct FanDevTables {
+  const double *scos, *ssin, *dcos, *dsin;
+};
+
+// Traces ray (view, det).  Mode 0: fill the header and count segments.
+// Mode 1: also write the decision words into the block-interleaved array.
+template <int kMode>
+__device__ void fan_trace_ray(const at_fan_geometry g, FanDevTables T, int view, int det, RayHdr *hdr,
+                              int *offgrid, uint32_t *bits, uint32_t word_stride) {
+  const int NX = g.n, NY = g.n;
+  const double vx = g.pixel_mm, vy = g.pixel_mm;
+  // ms2d.cpp:172-183
+  const double scos = T.scos[view], ssin = T.ssin[view];
+  const double dcos = T.dcos[det], dsin = T.dsin[det];
+  const double sx = g.sod_mm * scos + NX * vx / 2.0;
+  const double sy = g.sod_mm * ssin + NX * vy / 2.0;
+  const double dx = g.sdd_mm * (dcos * scos - dsin * ssin) + sx;
+  const double dy = g.sdd_mm * (dsin * scos + dcos * ssin) + sy;
+  // tracing.cpp:39-87
+  int index = 0;
+  const double ray_x = dx - sx, ray_y = dy - sy;
+  const double L = sqrt(ray_x * ray_x + ray_y * ray_y);
+  double lambda_min = 0.0, lambda_max = L;
+  const int signx = (ray_x > 0) ? 1 : -1;
+  const int signy = (ray_y > 0) ? 1 : -1;
+  const double absx = fabs(ray_x), absy = fabs(ray_y);
+  const double len_x = (absx > 1.e-4) ? (L / absx) * vx : 1.e6;
+  const double len_y = (absy > 1.e-4) ? (L / absy) * vy : 1.e6;
+  double tempx = NX * vx, tempy = NY * vy;
+  double l0, lN, temp;
+  l0 = (L * (0.0 - sx)) / (dx - sx);
+  lN = (L * (tempx - sx)) / (dx - sx);
+  temp = (l0 < lN) ? l0 : lN;
+  lambda_min = (lambda_min > temp) ? lambda_min : temp;
+  if (lambda_min == temp) index = 1;
+  temp = (l0 > lN) ? l0 : lN;
+  lambda_max = (lambda_max < temp) ? lambda_max : temp;
+  l0 = (L * (0.0 - sy)) / (dy - sy);
+  lN = (L * (tempy - sy)) / (dy - sy);
+  temp = (l0 < lN) ? l0 : lN;
+  lambda_min = (lambda_min > temp) ? lambda_min : temp;
+  if (lambda_min == temp) index = 2;
+  temp = (l0 > lN) ? l0 : lN;
+  lambda_max = (lambda_max < temp) ? lambda_max : temp;
+
+  RayHdr h;
+  h.pix0 = 0;
+  h.nseg = 0;
+  h.xy0 = 0;
+  h.sgn = (signx > 0 ? 1 : 0) | (signy > 0 ? 2 : 0);
+  h.ax = h.ay = 0.f;
+  h.lenx = (float)len_x;
+  h.leny = (float)len_y;
+  if (lambda_min >= lambda_max) {
+    if (kMode == 0) {
+      *hdr = h;
+      *offgrid = 0;
+    }
+    return;
+  }
+  double lambda0 = lambda_min, lambda_x, lambda_y;
+  int v_x, v_y;
+  if (index == 1) {  // tracing.cpp:91-102
+    v_x = (signx == 1) ? 0 : NX - 1;
+    lambda_x = lambda0 + len_x;
+    v_y = (int)((sy + lambda0 * ray_y / L) / vy);
+    tempy = v_y * vy;
+    lambda_y = (absy < 1.e-4) ? 1.e6 : (L * ((tempy + (signy > 0) * vy) - sy)) / (dy - sy);
+  } else {  // tracing.cpp:104-115
+    v_y = (signy == 1) ? 0 : NY - 1;
+    lambda_y = lambda0 + len_y;
+    v_x = (int)((sx + lambda0 * ray_x / L) / vx);
+    tempx = v_x * vx;
+    lambda_x = (absx < 1.e-4) ? 1.e6 : (L * ((tempx + (signx > 0) * vx) - sx)) / (dx - sx);
+  }
+  h.pix0 = v_x * NY + v_y;
+  h.xy0 = (v_x & 0xffff) | (v_y << 16);
+  h.ax = (float)(lambda_x - lambda_min);
+  h.ay = (float)(lambda_y - lambda_min);
+  int numb = 0, bad = 0;
+  uint32_t word = 0;
+  const double stop = lambda_max - 5.e-2;
+  while (lambda0 < stop) {  // tracing.cpp:118-146
+    if ((unsigned)v_x >= (unsigned)NX || (unsigned)v_y >= (unsigned)NY) bad++;
+    const bool xstep = lambda_x <= lambda_y;
+    if (kMode == 1) {
+      if (xstep) word |= 1u << (numb & 31);
+      if ((numb & 31) == 31) {
+        bits[(size_t)(numb >> 5) * word_stride] = word;
+        word = 0;
+      }
+    }
+    ++numb;
+    if (xstep) {
+      lambda0 = lambda_x;
+      lambda_x += len_x;
+      v_x += signx;
+    } else {
+      lambda0 = lambda_y;
+      lambda_y += len_y;
+      v_y += signy;
+    }
+  }
+  if (kMode == 1 && (numb & 31) != 0) bits[(size_t)(numb >> 5) * word_stride] = word;
+  if (kMode == 0) {
+    h.nseg = numb;
+    *hdr = h;
+    *offgrid = bad;
+  }
+}
+
+__global__ void fan_count_kernel(at_fan_geometry g, FanDevTables T, RayHdr *hdr, int *offgrid) {
+  const int ray = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ray >= g.nviews * g.ndets) return;
+  const int view = ray / g.ndets, det = ray % g.ndets;
+  fan_trace_ray<0>(g, T, view, det, hdr + ray, offgrid + ray, nullptr, 0);
+}
+
+__global__ void fan_fill_kernel(at_fan_geometry g, FanDevTables T, int nblocks_per_view, const uint32_t *blk_word,
+                                uint32_t *bits) {
+  const int ray = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ray >= g.nviews * g.ndets) return;
+  const int view = ray / g.ndets, det = ray % g.ndets;
+  const int blk = view * nblocks_per_view + det / kRayBlock;
+  uint32_t *dst = bits + blk_word[blk] + (det % kRayBlock);
+  fan_trace_ray<1>(g, T, view, det, nullptr, nullptr, dst, kRayBlock);
+}
+
+namespace {
+template <typename T>
+int dev_alloc(T **p, size_t count, int64_t &acct) {
+  cudaError_t e = cudaMalloc((void **)p, sizeof(T) * std::max<size_t>(count, 1));
+  if (e != cudaSuccess) return set_error(AT_ENOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  acct += (int64_t)(sizeof(T) * count);
+  return AT_OK;
+}
+}  // namespace
+
+int build_fan_plan(Plan &p, cudaStream_t st) {
+  const at_fan_geometry &g = p.geom;
+  const int nv = g.nviews, nd = g.ndets, nrays = nv * nd;
+  p.n = g.n;
+  p.nviews = nv;
+  p.ndets = nd;
+  p.rays = nrays;
+  std::vector<double> scos(nv), ssin(nv), dcos(nd), dsin(nd);
+  fan_tables(g, scos.data(), ssin.data(), dcos.data(), dsin.data());
+  double *tab_d = nullptr;
+  int rc;
+  AT_CUDA_TRY(cudaMalloc(&tab_d, sizeof(double) * 2 * (nv + nd)));
+  AT_CUDA_TRY(cudaMemcpyAsync(tab_d, scos.data(), sizeof(double) * nv, cudaMemcpyHostToDevice, st));
+  AT_CUDA_TRY(cudaMemcpyAsync(tab_d + nv, ssin.data(), sizeof(double) * nv, cudaMemcpyHostToDevice, st));
+  AT_CUDA_TRY(cudaMemcpyAsync(tab_d + 2 * nv, dcos.data(), sizeof(double) * nd, cudaMemcpyHostToDevice, st));
+  AT_CUDA_TRY(cudaMemcpyAsync(tab_d + 2 * nv + nd, dsin.data(), sizeof(double) * nd, cudaMemcpyHostToDevice, st));
+  FanDevTables T{tab_d, tab_d + nv, tab_d + 2 * nv, tab_d + 2 * nv + nd};
+
+  if ((rc = dev_alloc(&p.rays_d, nrays, p.device_bytes))) return rc;
+  int *off_d = nullptr;
+  AT_CUDA_TRY(cudaMalloc(&off_d, sizeof(int) * nrays));
+  const int tpb = 128;
+  fan_count_kernel<<<(nrays + tpb - 1) / tpb, tpb, 0, st>>>(g, T, p.rays_d, off_d);
+  AT_CUDA_TRY(cudaGetLastError());
+
+  std::vector<RayHdr> hdr(nrays);
+  std::vector<int> off(nrays);
+  AT_CUDA_TRY(cudaMemcpyAsync(hdr.data(), p.rays_d, sizeof(RayHdr) * nrays, cudaMemcpyDeviceToHost, st));
+  AT_CUDA_TRY(cudaMemcpyAsync(off.data(), off_d, sizeof(int) * nrays, cudaMemcpyDeviceToHost, st));
+  AT_CUDA_TRY(cudaStreamSynchronize(st));
+  cudaFree(off_d);
+
+  p.nblocks_per_view = (nd + kRayBlock - 1) / kRayBlock;
+  p.nblocks = nv * p.nblocks_per_view;
+  std::vector<uint32_t> blk_word(p.nblocks + 1);
+  std::vector<uint8_t> blk_nw(p.nblocks);
+  uint64_t words = 0;
+  int64_t segs = 0, bad = 0;
+  int maxseg = 0;
+  for (int v = 0; v < nv; v++)
+    for (int b = 0; b < p.nblocks_per_view; b++) {
+      int mx = 0;
+      for (int d = b * kRayBlock; d < std::min(nd, (b + 1) * kRayBlock); d++) {
+        const RayHdr &h = hdr[(size_t)v * nd + d];
+        mx = std::max(mx, h.nseg);
+        segs += h.nseg;
+        bad += off[(size_t)v * nd + d];
+      }
+      maxseg = std::max(maxseg, mx);
+      const int blk = v * p.nblocks_per_view + b;
+      const int nw = (mx + 31) / 32;
+      if (nw > 255) return set_error(AT_EINVAL, "ray longer than 8160 segments");
+      blk_word[blk] = (uint32_t)words;
+      blk_nw[blk] = (uint8_t)nw;
+      words += (uint64_t)nw * kRayBlock;
+    }
+  if (words >= (1ull << 32)) return set_error(AT_EINVAL, "plan exceeds 2^32 decision words");
+  blk_word[p.nblocks] = (uint32_t)words;
+  p.segments = segs;
+  p.offgrid = bad;
+  p.max_segments = maxseg;
+
+  if ((rc = dev_alloc(&p.bits_d, words, p.device_bytes))) return rc;
+  if ((rc = dev_alloc(&p.blk_word_d, p.nblocks + 1, p.device_bytes))) return rc;
+  if ((rc = dev_alloc(&p.blk_nw_d, p.nblocks, p.device_bytes))) return rc;
+  AT_CUDA_TRY(cudaMemsetAsync(p.bits_d, 0, sizeof(uint32_t) * std::max<uint64_t>(words, 1), st));
+  AT_CUDA_TRY(cudaMemcpyAsync(p.blk_word_d, blk_word.data(), sizeof(uint32_t) * (p.nblocks + 1),
+                              cudaMemcpyHostToDevice, st));
+  AT_CUDA_TRY(cudaMemcpyAsync(p.blk_nw_d, blk_nw.data(), p.nblocks, cudaMemcpyHostToDevice, st));
+  fan_fill_kernel<<<(nrays + tpb - 1) / tpb, tpb, 0, st>>>(g, T, p.nblocks_per_view, p.blk_word_d, p.bits_d);
+  AT_CUDA_TRY(cudaGetLastError());
+
+  // per-view source position and central direction for the back projector
+  std::vector<float4> views(nv);
+  for (int v = 0; v < nv; v++) {
+    const double sx = g.sod_mm * scos[v] + g.n * g.pixel_mm / 2.0;
+    const double sy = g.sod_mm * ssin[v] + g.n * g.pixel_mm / 2.0;
+    views[v] = make_float4((float)sx, (float)sy, (float)scos[v], (float)ssin[v]);
+  }
+  if ((rc = dev_alloc(&p.view_d, nv, p.device_bytes))) return rc;
+  AT_CUDA_TRY(cudaMemcpyAsync(p.view_d, views.data(), sizeof(float4) * nv, cudaMemcpyHostToDevice, st));
+  const double pitch_rad = g.det_pitch_deg * M_PI / 180.;
+  p.det_inv_pitch = (float)(1.0 / pitch_rad);
+  p.det_t0 = (float)(nd / 2 - g.off_center);
+  p.device_bytes += (int64_t)sizeof(RayHdr) * 0;  // headers already counted
+  AT_CUDA_TRY(cudaStreamSynchronize(st));
+  cudaFree(tab_d);
+  return AT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// GoldenC parallel beam
+// ---------------------------------------------------------------------------
+constexpr int kGcN = 512, kGcDets = 767, kGcTile = 128, kGcRays = 384, kGcAlphas = 45;
+constexpr int kGcPairs = kGcAlphas * kGcRays;  // (alpha, raynum) pairs
+constexpr int kGcWalks = kGcPairs * 16;        // (alpha, raynum, tile)
+
+struct GcTrig {
+  double sf, cf, hx, hy, tanphi, rtnphi;
+};
+
+// proj.c:55-200.  walk = pair*16 + tile.  Mode 0 counts, mode 1 writes.
+template <int kMode>
+__device__ int gc_walk_dev(const GcTrig *trig, int walk, GcSeg *out) {
+  const int pair = walk >> 4, tile = walk & 15;
+  const int alpha = 1 + pair / kGcRays, raynum = pair % kGcRays;
+  const GcTrig t = trig[alpha - 1];
+  const int ind = raynum - (kGcDets / 2);
+  const int col = tile % 4;
+  const int dxo = kGcTile * (3 - col), dyo = kGcTile * (tile / 4);
+  double c = t.cf * ind + t.sf * ind * t.tanphi;
+  c = (kGcN / 2 - dyo) - t.tanphi * (kGcN / 2 - kGcTile * col) - c;
+  int ix, iy, next;
+  double fp, w, xc, yc;
+  if (c < 0) {
+    c = -c * t.rtnphi;
+    ix = (int)c;
+    iy = 0;
+    fp = ((double)(ix + 1)) - c;
+    ix = kGcTile - ix - 1;
+    w = t.hy * fp;
+    yc = fp * t.tanphi;
+    xc = -fp;
+    next = 2;
+  } else {
+    ix = kGcTile - 1;
+    iy = (int)c;
+    fp = ((double)(iy + 1)) - c;
+    yc = -fp;
+    w = t.hx * fp;
+    xc = fp * t.rtnphi;
+    next = 1;
+  }
+  int n = 0;
+  while (ix >= 0 && ix < kGcTile && iy >= 0 && iy < kGcTile) {
+    double emit;
+    const int ex = ix, ey = iy;
+    if (next == 1) {
+      xc -= 1.0;
+      yc += t.tanphi;
+      if (xc > 0) {
+        emit = t.hy;
+        w -= t.hy;
+        ix -= 1;
+      } else {
+        emit = w;
+        w = t.hy - w;
+        iy++;
+        next = 2;
+      }
+    } else {
+      yc -= 1.0;
+      xc += t.rtnphi;
+      if (yc > 0) {
+        w -= t.hx;
+        emit = t.hx;
+        iy++;
+      } else {
+        emit = w;
+        w = t.hx - w;
+        ix -= 1;
+        next = 1;
+      }
+    }
+    if (kMode == 1) {
+      out[n].pix = (ey + dyo) * kGcN + (ex + dxo);
+      out[n].w = (float)emit;
+    }
+    n++;
+  }
+  return n;
+}
+
+__global__ void gc_count_kernel(const GcTrig *trig, int *count) {
+  const int walk = blockIdx.x * blockDim.x + threadIdx.x;
+  if (walk >= kGcWalks) return;
+  count[walk] = gc_walk_dev<0>(trig, walk, nullptr);
+}
+
+__global__ void gc_fill_kernel(const GcTrig *trig, const int64_t *walk_off, GcSeg *seg) {
+  const int walk = blockIdx.x * blockDim.x + threadIdx.x;
+  if (walk >= kGcWalks) return;
+  gc_walk_dev<1>(trig, walk, seg + walk_off[walk]);
+}
+
+__global__ void gc_pix_count_kernel(const GcSeg *seg, int64_t nseg, int *cnt) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= nseg) return;
+  atomicAdd(&cnt[seg[i].pix], 1);
+}
+
+__global__ void gc_pix_fill_kernel(const GcSeg *seg, const int32_t *pair_off, int64_t nseg, int *cursor,
+                                   GcEntry *ent) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= nseg) return;
+  // pair of segment i: binary search in pair_off
+  int lo = 0, hi = kGcPairs;  // pair_off[lo] <= i < pair_off[hi]
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (pair_off[mid] <= i) lo = mid;
+    else hi = mid;
+  }
+  const int pos = atomicAdd(&cursor[seg[i].pix], 1);
+  ent[pos].pair = lo;
+  ent[pos].w = seg[i].w;
+}
+
+// orders each pixel's entries by pair so the gather sums in a fixed order
+__global__ void gc_pix_sort_kernel(const int32_t *pix_off, GcEntry *ent) {
+  const int pix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix >= kGcN * kGcN) return;
+  const int b = pix_off[pix], e = pix_off[pix + 1];
+  for (int i = b + 1; i < e; i++) {
+    const GcEntry x = ent[i];
+    int j = i - 1;
+    while (j >= b && ent[j].pair > x.pair) {
+      ent[j + 1] = ent[j];
+      j--;
+    }
+    ent[j + 1] = x;
+  }
+}
+
+int build_goldnc_plan(Plan &p, cudaStream_t st) {
+  p.kind = AT_GEOM_GOLDNC;
+  p.n = kGcN;
+  p.nviews = 180;
+  p.ndets = kGcDets;
+  p.rays = 180 * kGcDets;
+  std::vector<GcTrig> trig(kGcAlphas);
+  for (int a = 1; a <= kGcAlphas; a++) {  // proj.c:43-48, host libm
+    GcTrig &t = trig[a - 1];
+    const double ang = 3.141593 / 180 * a;
+    t.sf = std::sin(ang);
+    t.cf = std::cos(ang);
+    t.hx = ((double)1.0) / t.sf;
+    t.hy = ((double)1.0) / t.cf;
+    t.tanphi = t.sf / t.cf;
+    t.rtnphi = t.cf / t.sf;
+  }
+  GcTrig *trig_d = nullptr;
+  int *cnt_d = nullptr;
+  AT_CUDA_TRY(cudaMalloc(&trig_d, sizeof(GcTrig) * kGcAlphas));
+  AT_CUDA_TRY(cudaMemcpyAsync(trig_d, trig.data(), sizeof(GcTrig) * kGcAlphas, cudaMemcpyHostToDevice, st));
+  AT_CUDA_TRY(cudaMalloc(&cnt_d, sizeof(int) * kGcWalks));
+  gc_count_kernel<<<(kGcWalks + 127) / 128, 128, 0, st>>>(trig_d, cnt_d);
+  AT_CUDA_TRY(cudaGetLastError());
+  std::vector<int> cnt(kGcWalks);
+  AT_CUDA_TRY(cudaMemcpyAsync(cnt.data(), cnt_d, sizeof(int) * kGcWalks, cudaMemcpyDeviceToHost, st));
+  AT_CUDA_TRY(cudaStreamSynchronize(st));
+  std::vector<int64_t> walk_off(kGcWalks + 1);
+  std::vector<int32_t> pair_off(kGcPairs + 1);
+  int64_t tot = 0;
+  int maxseg = 0;
+  for (int w = 0; w < kGcWalks; w++) {
+    if ((w & 15) == 0) pair_off[w >> 4] = (int32_t)tot;
+    walk_off[w] = tot;
+    tot += cnt[w];
+  }
+  walk_off[kGcWalks] = tot;
+  pair_off[kGcPairs] = (int32_t)tot;
+  for (int q = 0; q < kGcPairs; q++) maxseg = std::max(maxseg, pair_off[q + 1] - pair_off[q]);
+  p.max_segments = maxseg;
+  p.segments = tot;  // traced segments (each feeds up to 8 bins)
+  int rc;
+  int64_t *walk_off_d = nullptr;
+  AT_CUDA_TRY(cudaMalloc(&walk_off_d, sizeof(int64_t) * (kGcWalks + 1)));
+  AT_CUDA_TRY(cudaMemcpyAsync(walk_off_d, walk_off.data(), sizeof(int64_t) * (kGcWalks + 1),
+                              cudaMemcpyHostToDevice, st));
+  if ((rc = dev_alloc(&p.gc_seg_d, tot, p.device_bytes))) return rc;
+  if ((rc = dev_alloc(&p.gc_pair_off_d, kGcPairs + 1, p.device_bytes))) return rc;
+  AT_CUDA_TRY(cudaMemcpyAsync(p.gc_pair_off_d, pair_off.data(), sizeof(int32_t) * (kGcPairs + 1),
+                              cudaMemcpyHostToDevice, st));
+  gc_fill_kernel<<<(kGcWalks + 127) / 128, 128, 0, st>>>(trig_d, walk_off_d, p.gc_seg_d);
+  AT_CUDA_TRY(cudaGetLastError());
+
+  // transpose to per-pixel lists
+  int *pcnt_d = nullptr;
+  AT_CUDA_TRY(cudaMalloc(&pcnt_d, sizeof(int) * kGcN * kGcN));
+  AT_CUDA_TRY(cudaMemsetAsync(pcnt_d, 0, sizeof(int) * kGcN * kGcN, st));
+  const int nb = (int)((tot + 255) / 256);
+  gc_pix_count_kernel<<<nb, 256, 0, st>>>(p.gc_seg_d, tot, pcnt_d);
+  AT_CUDA_TRY(cudaGetLastError());
+  std::vector<int> pcnt(kGcN * kGcN);
+  AT_CUDA_TRY(cudaMemcpyAsync(pcnt.data(), pcnt_d, sizeof(int) * kGcN * kGcN, cudaMemcpyDeviceToHost, st));
+  AT_CUDA_TRY(cudaStreamSynchronize(st));
+  std::vector<int32_t> pix_off(kGcN * kGcN + 1);
+  int64_t acc = 0;
+  for (int i = 0; i < kGcN * kGcN; i++) {
+    pix_off[i] = (int32_t)acc;
+    acc += pcnt[i];
+  }
+  pix_off[kGcN * kGcN] = (int32_t)acc;
+  if ((rc = dev_alloc(&p.gc_pix_off_d, kGcN * kGcN + 1, p.device_bytes))) return rc;
+  if ((rc = dev_alloc(&p.gc_ent_d, tot, p.device_bytes))) return rc;
+  AT_CUDA_TRY(cudaMemcpyAsync(p.gc_pix_off_d, pix_off.data(), sizeof(int32_t) * (kGcN * kGcN + 1),
+                              cudaMemcpyHostToDevice, st));
+  AT_CUDA_TRY(cudaMemcpyAsync(pcnt_d, pix_off.data(), sizeof(int32_t) * kGcN * kGcN, cudaMemcpyHostToDevice, st));
+  gc_pix_fill_kernel<<<nb, 256, 0, st>>>(p.gc_seg_d, p.gc_pair_off_d, tot, pcnt_d, p.gc_ent_d);
+  AT_CUDA_TRY(cudaGetLastError());
+  gc_pix_sort_kernel<<<(kGcN * kGcN + 255) / 256, 256, 0, st>>>(p.gc_pix_off_d, p.gc_ent_d);
+  AT_CUDA_TRY(cudaGetLastError());
+  AT_CUDA_TRY(cudaStreamSynchronize(st));
+  cudaFree(pcnt_d);
+  cudaFree(walk_off_d);
+  cudaFree(cnt_d);
+  cudaFree(trig_d);
+  return AT_OK;
+}
+
+Plan::~Plan() {
+  cudaFree(rays_d);
+  cudaFree(bits_d);
+  cudaFree(blk_word_d);
+  cudaFree(blk_nw_d);
+  cudaFree(view_d);
+  cudaFree(gc_seg_d);
+  cudaFree(gc_pair_off_d);
+  cudaFree(gc_ent_d);
+  cudaFree(gc_pix_off_d);
+}
+
+}  // namespace at

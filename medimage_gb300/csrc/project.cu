@@ -1,0 +1,439 @@
+// project.cu -- forward (A f) and back (A^T r) projection kernels with the
+// solver's fused epilogues.
+//
+// Fan beam, forward: each thread walks RPT adjacent rays of one view through
+// the plan's decision bits (1 bit per segment, block-interleaved so a warp's
+// word loads are coalesced), reads the traversed pixels through the read-only
+// cache, accumulates FP32 products per 32-segment word and folds the word sums
+// into a Kahan-compensated total.  The traversal (pixel sequence) is the
+// reference's FP64 one (helical/rebin/src/tracing.cpp:118-146); weights are
+// differences of FP32 boundary crossings.
+// Fan beam, back: one thread per pixel gathers, view by view, the few rays
+// whose plan passes through the pixel, with the same FP32 crossing formula the
+// forward walk uses, so A^T is the transpose of A up to FP32 rounding, and no
+// atomics are involved (deterministic).
+// GoldenC: forward = one warp per traced (alpha, raynum) pair summing its 16
+// tile walks into the 8 symmetric bins of proj.c:114-127; back = one thread
+// per pixel over the transposed walk lists, with the 90-degree column of
+// proj.c:225.
+#include <cuda_runtime.h>
+
+#include "solver_dev.cuh"
+
+namespace at {
+
+// ---------------------------------------------------------------------------
+// epilogues
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void fp_epilogue(const ScanDev &S, const Launch &L, int bin, float val, double &s0) {
+  switch (L.stage) {
+    case ST_FP0: {  // r = g - Af ; E_data
+      const float g = S.buf[B_G][bin];
+      S.buf[B_R][bin] = g - val;
+      const double dv = (double)val - (double)g;
+      s0 += dv * dv;
+      if (L.aux_buf >= 0) S.buf[L.aux_buf][bin] = val;
+      break;
+    }
+    case ST_FPQ:  // q = A p ; |q|^2
+      S.buf[B_Q][bin] = val;
+      s0 += (double)val * (double)val;
+      break;
+    case ST_FPA: {  // E_data ; r -= c1 q
+      const float g = S.buf[B_G][bin];
+      const double dv = (double)val - (double)g;
+      s0 += dv * dv;
+      const float c1 = (float)S.ctl->c1;
+      S.buf[B_R][bin] = S.buf[B_R][bin] - c1 * S.buf[B_Q][bin];
+      if (L.aux_buf >= 0) S.buf[L.aux_buf][bin] = val;
+      break;
+    }
+    case ST_FPD:  // <A d, q>
+      s0 += (double)val * (double)S.buf[B_Q][bin];
+      if (L.aux_buf >= 0) S.buf[L.aux_buf][bin] = val;
+      break;
+    default:
+      S.buf[L.out_buf][bin] = val;
+      break;
+  }
+}
+
+__device__ __forceinline__ bool stage_reduces(int stage) {
+  return stage == ST_FP0 || stage == ST_FPQ || stage == ST_FPA || stage == ST_FPD || stage == ST_BP0 ||
+         stage == ST_BPD;
+}
+
+// d = A^T r + alpha * div-stencil (main.c:112-125, 226-239) and the smoothness
+// energy over the interior (main.c:135-139, 203-208).
+__device__ __forceinline__ void bp_epilogue(const ScanDev &S, const Launch &L, int x, int y, float val, double &s0) {
+  const int n = S.n;
+  const int i = x * n + y;
+  if (L.stage != ST_BP0 && L.stage != ST_BPD) {
+    S.buf[L.out_buf][i] = val;
+    return;
+  }
+  const float *u = S.buf[L.aux_buf];  // the update the stencil acts on
+  const float *v = S.buf[B_V];
+  const Ctl *c = S.ctl;
+  const float alpha = (float)c->alpha;
+  const float eps2 = (float)(0.01 * c->eps * c->eps);
+  const float Pc = v[i];
+  const float Pu = x > 0 ? v[i - n] : 1.f;
+  const float Pl = y > 0 ? v[i - 1] : 1.f;
+  const float Tc = u[i];
+  const float Td = x + 1 < n ? u[i + n] : 0.f;
+  const float Tr = y + 1 < n ? u[i + 1] : 0.f;
+  const float Tu = x > 0 ? u[i - n] : 0.f;
+  const float Tl = y > 0 ? u[i - 1] : 0.f;
+  const float Pc2 = Pc * Pc;
+  const float st = Pc2 * (Td - Tc) + Pc2 * (Tr - Tc) - Pu * Pu * (Tc - Tu) - Pl * Pl * (Tc - Tl) +
+                   eps2 * (Td + Tr - 4.f * Tc + Tu + Tl);
+  S.buf[B_D][i] = val + alpha * st;
+  if (x >= 1 && x <= n - 2 && y >= 1 && y <= n - 2) {
+    const double a = (double)Tc - (double)Tu, b = (double)Tc - (double)Tl;
+    s0 += (double)alpha * ((double)Pc2 + (double)eps2) * (a * a + b * b);
+  }
+}
+
+__device__ __forceinline__ void kahan_add(float &sum, float &comp, float x) {
+  const float y = x - comp;
+  const float t = sum + y;
+  comp = (t - sum) - y;
+  sum = t;
+}
+
+// ---------------------------------------------------------------------------
+// fan-beam forward projection
+// ---------------------------------------------------------------------------
+template <int RPT>
+__global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
+  const int scan = L.scans ? find_scan(L.prefix, L.nscans, blockIdx.x) : 0;
+  const ScanDev &S = scan_of(L, scan);
+  if (!flow_active(S, L.flow)) return;
+  const int cta0 = L.scans ? __ldg(L.prefix + scan) : 0;
+  const int ncta = L.scans ? __ldg(L.prefix + scan + 1) - cta0 : gridDim.x;
+  const int local_cta = blockIdx.x - cta0;
+  constexpr int kWarpsPerBlock = 4 / RPT;  // warps per 128-ray bit block
+  const int lane = threadIdx.x & 31;
+  const int lw = local_cta * 4 + (threadIdx.x >> 5);
+  const int blk = lw / kWarpsPerBlock, slice = lw % kWarpsPerBlock;
+  const int nblk = S.nviews * S.nbpv;
+  double s0 = 0.0;
+  if (blk < nblk) {
+    const int view = blk / S.nbpv;
+    const int in_blk = slice * 32 * RPT + lane * RPT;  // first ray of this thread within the block
+    const int det0 = (blk % S.nbpv) * kRayBlock + in_blk;
+    const float *__restrict__ img = S.buf[L.in_buf];
+    const unsigned npix = (unsigned)S.npix;
+    int idx[RPT], stx[RPT], sty[RPT], nseg[RPT];
+    float ax[RPT], ay[RPT], lx[RPT], ly[RPT], cx[RPT], cy[RPT], prev[RPT], acc[RPT], comp[RPT];
+    int my_max = 0;
+#pragma unroll
+    for (int r = 0; r < RPT; r++) {
+      const int det = det0 + r;
+      nseg[r] = 0;
+      idx[r] = 0;
+      stx[r] = sty[r] = 0;
+      ax[r] = ay[r] = lx[r] = ly[r] = 0.f;
+      if (det < S.ndets) {
+        const uint4 *hp = reinterpret_cast<const uint4 *>(S.rays + (size_t)view * S.ndets + det);
+        const uint4 h0 = __ldg(hp), h1 = __ldg(hp + 1);
+        idx[r] = (int)h0.x;
+        nseg[r] = (int)h0.y;
+        stx[r] = (h0.w & 1u) ? S.n : -S.n;
+        sty[r] = (h0.w & 2u) ? 1 : -1;
+        ax[r] = __uint_as_float(h1.x);
+        ay[r] = __uint_as_float(h1.y);
+        lx[r] = __uint_as_float(h1.z);
+        ly[r] = __uint_as_float(h1.w);
+      }
+      cx[r] = cy[r] = prev[r] = acc[r] = comp[r] = 0.f;
+      my_max = max(my_max, nseg[r]);
+    }
+    // warp-uniform trip count
+    unsigned mm = (unsigned)my_max;
+    mm = __reduce_max_sync(0xffffffffu, mm);
+    const int nwords = ((int)mm + 31) >> 5;
+    const uint32_t *wp = S.bits + __ldg(S.blk_word + blk) + in_blk;
+    for (int w = 0; w < nwords; w++) {
+      uint32_t bw[RPT];
+      if constexpr (RPT == 4) {
+        const uint4 t = __ldg(reinterpret_cast<const uint4 *>(wp + (size_t)w * kRayBlock));
+        bw[0] = t.x;
+        bw[1] = t.y;
+        bw[2] = t.z;
+        bw[3] = t.w;
+      } else if constexpr (RPT == 2) {
+        const uint2 t = __ldg(reinterpret_cast<const uint2 *>(wp + (size_t)w * kRayBlock));
+        bw[0] = t.x;
+        bw[1] = t.y;
+      } else {
+        bw[0] = __ldg(wp + (size_t)w * kRayBlock);
+      }
+      float part[RPT];
+#pragma unroll
+      for (int r = 0; r < RPT; r++) part[r] = 0.f;
+      const int base = w << 5;
+#pragma unroll 8
+      for (int b = 0; b < 32; b++) {
+#pragma unroll
+        for (int r = 0; r < RPT; r++) {
+          const bool bx = (bw[r] >> b) & 1u;
+          const float nx = fmaf(cx[r], lx[r], ax[r]);
+          const float ny = fmaf(cy[r], ly[r], ay[r]);
+          const float cur = bx ? nx : ny;
+          const float wt = cur - prev[r];
+          prev[r] = cur;
+          const bool on = (base + b) < nseg[r] && (unsigned)idx[r] < npix;
+          const float val = on ? __ldg(img + idx[r]) : 0.f;
+          part[r] = fmaf(wt, val, part[r]);
+          idx[r] += bx ? stx[r] : sty[r];
+          cx[r] += bx ? 1.f : 0.f;
+          cy[r] += bx ? 0.f : 1.f;
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < RPT; r++) kahan_add(acc[r], comp[r], part[r]);
+    }
+    const int row0 = view * S.ndets;
+#pragma unroll
+    for (int r = 0; r < RPT; r++) {
+      const int det = det0 + r;
+      if (det < S.ndets) fp_epilogue(S, L, row0 + det, acc[r] - comp[r], s0);
+    }
+  }
+  if (stage_reduces(L.stage)) {
+    double v[1] = {s0};
+    reduce_and_finalize<1>(S, L, v, local_cta, ncta);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// fan-beam back projection (gather)
+// ---------------------------------------------------------------------------
+// CTA = 8 x 32 pixel tile (x rows by y columns), one pixel per thread.
+__global__ void __launch_bounds__(256) fan_bp_kernel(const Launch L) {
+  const int scan = L.scans ? find_scan(L.prefix, L.nscans, blockIdx.x) : 0;
+  const ScanDev &S = scan_of(L, scan);
+  if (!flow_active(S, L.flow)) return;
+  const int cta0 = L.scans ? __ldg(L.prefix + scan) : 0;
+  const int ncta = L.scans ? __ldg(L.prefix + scan + 1) - cta0 : gridDim.x;
+  const int local_cta = blockIdx.x - cta0;
+  const int n = S.n;
+  const int tiles_y = (n + 31) >> 5;
+  const int x = (local_cta / tiles_y) * 8 + (threadIdx.x >> 5);
+  const int y = (local_cta % tiles_y) * 32 + (threadIdx.x & 31);
+  const bool inside = x < n && y < n;
+  const float *__restrict__ sino = S.buf[L.in_buf];
+  const float px = S.pixel_mm;
+  const float Px = (x + 0.5f) * px, Py = (y + 0.5f) * px;
+  const float half = 0.5f * px, diag = 0.70711f * px;
+  float acc = 0.f, comp = 0.f;
+  if (inside) {
+    for (int view = 0; view < S.nviews; view++) {
+      const float4 vw = __ldg(S.view + view);  // sx, sy, cos(beta), sin(beta)
+      const float Dx = Px - vw.x, Dy = Py - vw.y;
+      const float along = -(Dx * vw.z + Dy * vw.w);
+      const float perp = Dx * vw.w - Dy * vw.z;
+      const float t = atanf(perp / along) * S.det_inv_pitch + S.det_t0;
+      const float dist = sqrtf(along * along + perp * perp);
+      const float h = half * (fabsf(Dx) + fabsf(Dy)) / dist / (dist - diag) * S.det_inv_pitch + 1e-3f;
+      const int jlo = max(0, (int)ceilf(t - h));
+      const int jhi = min(S.ndets - 1, (int)floorf(t + h));
+      float contrib = 0.f;
+      for (int j = jlo; j <= jhi; j++) {
+        const uint4 *hp = reinterpret_cast<const uint4 *>(S.rays + (size_t)view * S.ndets + j);
+        const uint4 h0 = __ldg(hp);
+        const int x0 = (int)(h0.z & 0xffffu), y0 = (int)(h0.z >> 16);
+        const int cx = (h0.w & 1u) ? x - x0 : x0 - x;
+        const int cy = (h0.w & 2u) ? y - y0 : y0 - y;
+        if (cx < 0 || cy < 0 || cx + cy >= (int)h0.y) continue;
+        const uint4 h1 = __ldg(hp + 1);
+        const float ax = __uint_as_float(h1.x), ay = __uint_as_float(h1.y);
+        const float lx = __uint_as_float(h1.z), ly = __uint_as_float(h1.w);
+        const float fcx = (float)cx, fcy = (float)cy;
+        const float ex = fmaf(fcx, lx, ax), ey = fmaf(fcy, ly, ay);
+        const float ix = cx > 0 ? fmaf(fcx - 1.f, lx, ax) : 0.f;
+        const float iy = cy > 0 ? fmaf(fcy - 1.f, ly, ay) : 0.f;
+        const float wt = fminf(ex, ey) - fmaxf(ix, iy);
+        if (wt > 0.f) contrib = fmaf(wt, __ldg(sino + (size_t)view * S.ndets + j), contrib);
+      }
+      kahan_add(acc, comp, contrib);
+    }
+  }
+  double s0 = 0.0;
+  if (inside) bp_epilogue(S, L, x, y, acc - comp, s0);
+  if (stage_reduces(L.stage)) {
+    double v[1] = {s0};
+    reduce_and_finalize<1>(S, L, v, local_cta, ncta);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// GoldenC parallel beam
+// ---------------------------------------------------------------------------
+constexpr int kGcN = 512, kGcDets = 767, kGcRays = 384, kGcPairs = 45 * 384;
+constexpr int kGcLast = kGcN - 1;
+constexpr int kGcSpecial = 2 * kGcDets;  // bins of views 0 and 90
+constexpr int kGcFpWarps = kGcPairs + kGcSpecial;
+
+__device__ __forceinline__ int gc_sym_pix(int s, int X, int Y) {
+  switch (s) {  // proj.c:114-127 image samples
+    case 0: return Y * kGcN + X;
+    case 1: return (kGcLast - X) * kGcN + Y;
+    case 2: return (kGcLast - Y) * kGcN + (kGcLast - X);
+    case 3: return X * kGcN + (kGcLast - Y);
+    case 4: return X * kGcN + Y;
+    case 5: return (kGcLast - Y) * kGcN + X;
+    case 6: return (kGcLast - X) * kGcN + (kGcLast - Y);
+    default: return Y * kGcN + (kGcLast - X);
+  }
+}
+
+__device__ __forceinline__ bool gc_sym_present(int s, int a, int r) {
+  return !(((s & 2) && r == 383) || (s >= 4 && a == 45));
+}
+
+__device__ __forceinline__ int gc_sym_bin(int s, int a, int r) {
+  const int view = (s < 4) ? ((s & 1) ? 90 + a : a) : ((s & 1) ? 180 - a : 90 - a);
+  const int det = (s & 2) ? (kGcDets - 1 - r) : r;
+  return view * kGcDets + det;
+}
+
+__global__ void __launch_bounds__(128) gc_fp_kernel(const Launch L) {
+  const int scan = L.scans ? find_scan(L.prefix, L.nscans, blockIdx.x) : 0;
+  const ScanDev &S = scan_of(L, scan);
+  if (!flow_active(S, L.flow)) return;
+  const int cta0 = L.scans ? __ldg(L.prefix + scan) : 0;
+  const int ncta = L.scans ? __ldg(L.prefix + scan + 1) - cta0 : gridDim.x;
+  const int local_cta = blockIdx.x - cta0;
+  const int lane = threadIdx.x & 31;
+  const int gw = local_cta * 4 + (threadIdx.x >> 5);
+  const float *__restrict__ img = S.buf[L.in_buf];
+  double s0 = 0.0;
+  if (gw < kGcPairs) {
+    const int a = 1 + gw / kGcRays, r = gw % kGcRays;
+    float acc[8];
+#pragma unroll
+    for (int s = 0; s < 8; s++) acc[s] = 0.f;
+    const int b = __ldg(S.gc_pair_off + gw), e = __ldg(S.gc_pair_off + gw + 1);
+    for (int i = b + lane; i < e; i += 32) {
+      const int2 sg = __ldg(reinterpret_cast<const int2 *>(S.gc_seg) + i);
+      const int X = sg.x % kGcN, Y = sg.x / kGcN;
+      const float w = __int_as_float(sg.y);
+#pragma unroll
+      for (int s = 0; s < 8; s++) acc[s] = fmaf(__ldg(img + gc_sym_pix(s, X, Y)), w, acc[s]);
+    }
+#pragma unroll
+    for (int s = 0; s < 8; s++)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc[s] += __shfl_xor_sync(0xffffffffu, acc[s], o);
+#pragma unroll
+    for (int s = 0; s < 8; s++)
+      if (lane == s && gc_sym_present(s, a, r)) fp_epilogue(S, L, gc_sym_bin(s, a, r), acc[s], s0);
+  } else if (gw < kGcFpWarps) {
+    // views 0 (row sums, proj.c:17-26) and 90 (column sums at 256+ind, proj.c:27-36)
+    const int q = gw - kGcPairs;
+    const int view = q < kGcDets ? 0 : 90;
+    const int r = q % kGcDets;
+    const int ind = r - kGcDets / 2;
+    float acc = 0.f;
+    if (ind <= kGcN / 2 - 1 && ind >= 1 - kGcN / 2) {
+      if (view == 0) {
+        const float *row = img + (kGcN / 2 - 1 + ind) * kGcN;
+        for (int t = lane; t < kGcN; t += 32) acc += __ldg(row + t);
+      } else {
+        const int col = kGcN / 2 + ind;
+        for (int t = lane; t < kGcN; t += 32) acc += __ldg(img + t * kGcN + col);
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) fp_epilogue(S, L, view * kGcDets + r, acc, s0);
+  }
+  if (stage_reduces(L.stage)) {
+    double v[1] = {s0};
+    reduce_and_finalize<1>(S, L, v, local_cta, ncta);
+  }
+}
+
+__global__ void __launch_bounds__(256) gc_bp_kernel(const Launch L) {
+  const int scan = L.scans ? find_scan(L.prefix, L.nscans, blockIdx.x) : 0;
+  const ScanDev &S = scan_of(L, scan);
+  if (!flow_active(S, L.flow)) return;
+  const int cta0 = L.scans ? __ldg(L.prefix + scan) : 0;
+  const int ncta = L.scans ? __ldg(L.prefix + scan + 1) - cta0 : gridDim.x;
+  const int local_cta = blockIdx.x - cta0;
+  const int x = (local_cta >> 4) * 8 + (threadIdx.x >> 5);  // row
+  const int y = (local_cta & 15) * 32 + (threadIdx.x & 31); // column
+  const float *__restrict__ sino = S.buf[L.in_buf];
+  float acc = 0.f, comp = 0.f;
+  // views 0 and 90 (proj.c:210-230; column 255+ind at 90 degrees)
+  if (x <= kGcN - 2) acc += __ldg(sino + 0 * kGcDets + x + 128);
+  if (y <= kGcN - 2) acc += __ldg(sino + 90 * kGcDets + y + 128);
+#pragma unroll 1
+  for (int s = 0; s < 8; s++) {
+    int X, Y;  // symmetry-0 pixel whose image under s is (x, y)
+    switch (s) {
+      case 0: Y = x; X = y; break;
+      case 1: X = kGcLast - x; Y = y; break;
+      case 2: Y = kGcLast - x; X = kGcLast - y; break;
+      case 3: X = x; Y = kGcLast - y; break;
+      case 4: X = x; Y = y; break;
+      case 5: Y = kGcLast - x; X = y; break;
+      case 6: X = kGcLast - x; Y = kGcLast - y; break;
+      default: Y = x; X = kGcLast - y; break;
+    }
+    const int p = Y * kGcN + X;
+    const int b = __ldg(S.gc_pix_off + p), e = __ldg(S.gc_pix_off + p + 1);
+    float part = 0.f;
+    for (int i = b; i < e; i++) {
+      const int2 en = __ldg(reinterpret_cast<const int2 *>(S.gc_ent) + i);
+      const int a = 1 + en.x / kGcRays, r = en.x % kGcRays;
+      if (!gc_sym_present(s, a, r)) continue;
+      part = fmaf(__ldg(sino + gc_sym_bin(s, a, r)), __int_as_float(en.y), part);
+    }
+    kahan_add(acc, comp, part);
+  }
+  double s0 = 0.0;
+  bp_epilogue(S, L, x, y, acc - comp, s0);
+  if (stage_reduces(L.stage)) {
+    double v[1] = {s0};
+    reduce_and_finalize<1>(S, L, v, local_cta, ncta);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// launch helpers
+// ---------------------------------------------------------------------------
+int fp_ctas(const ScanDev &S, int rpt) {
+  if (S.kind == AT_GEOM_GOLDNC) return (kGcFpWarps + 3) / 4;
+  const int warps = S.nviews * S.nbpv * (4 / rpt);
+  return (warps + 3) / 4;
+}
+
+int bp_ctas(const ScanDev &S) {
+  if (S.kind == AT_GEOM_GOLDNC) return (kGcN / 8) * (kGcN / 32);
+  return ((S.n + 7) / 8) * ((S.n + 31) / 32);
+}
+
+cudaError_t launch_fp(const Launch &L, int kind, int rpt, int nctas, cudaStream_t st) {
+  if (kind == AT_GEOM_GOLDNC) {
+    gc_fp_kernel<<<nctas, 128, 0, st>>>(L);
+  } else if (rpt == 4) {
+    fan_fp_kernel<4><<<nctas, 128, 0, st>>>(L);
+  } else if (rpt == 2) {
+    fan_fp_kernel<2><<<nctas, 128, 0, st>>>(L);
+  } else {
+    fan_fp_kernel<1><<<nctas, 128, 0, st>>>(L);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bp(const Launch &L, int kind, int nctas, cudaStream_t st) {
+  if (kind == AT_GEOM_GOLDNC) gc_bp_kernel<<<nctas, 256, 0, st>>>(L);
+  else fan_bp_kernel<<<nctas, 256, 0, st>>>(L);
+  return cudaGetLastError();
+}
+
+}  // namespace at

@@ -1,0 +1,316 @@
+// solver_dev.cuh -- device-side state of a batch of scans and the control
+// logic of the AT iteration (origin/GoldenC/src/main.c:81-360), shared by the
+// projector kernels (which carry fused epilogues) and the pixel-pass kernels.
+//
+// Every kernel of the solver takes the whole batch.  A CTA belongs to exactly
+// one scan (per-scan CTA ranges come from a prefix table), returns at once if
+// that scan's step is no longer active, reduces its partial sums in FP64 and
+// writes them to the scan's partial array; the last CTA of the scan to arrive
+// sums the partials in a fixed order (deterministic) and runs the scalar part
+// of the step (line searches, exit tests) on the device.
+#pragma once
+
+#include <cstdint>
+
+#include "at_internal.h"
+
+namespace at {
+
+// image-shaped buffers, then sinogram-shaped buffers
+enum Buf : int {
+  B_F = 0,  // f (the image result; also update buffer 0)
+  B_U1,     // update buffer 1
+  B_V,      // edge field v
+  B_D,      // d (image-step gradient / edge-step direction)
+  B_P0,     // CG direction p, ping
+  B_P1,     // CG direction p, pong
+  B_NN,     // |grad f|^2 for the edge step
+  B_NIMG,
+  B_G = B_NIMG,  // sinogram data g
+  B_R,           // residual r
+  B_Q,           // q = A p
+  B_AF,          // A f   (linear mode)
+  B_AD,          // A d   (linear mode)
+  B_NBUF
+};
+
+// what a kernel launch belongs to: gates it on the scan's control flags
+enum Flow : int { FLOW_ALWAYS = 0, FLOW_IMAGE = 1, FLOW_EDGE = 2, FLOW_ENABLED = 3 };
+
+// stages whose reductions end in a scalar update
+enum Stage : int {
+  ST_NONE = 0,
+  ST_FP0,   // A(update): E_data, r = g - Af                       main.c:101-104,126-129
+  ST_BP0,   // A^T r + stencil: E_smooth -> AT_f_old               main.c:110-139
+  ST_PP0,   // p = d: nV, <p,d>                                    main.c:141-166
+  ST_FPQ,   // q = A p: |q|^2 -> c1                                main.c:146,163-167
+  ST_UPD,   // update += c1 p (+median): maxCP, exits              main.c:169-191
+  ST_FPA,   // A(update): E_data; r -= c1 q                        main.c:193-197,217-219
+  ST_BPD,   // A^T r + stencil: E_smooth -> AT_f_new, revert test  main.c:199-216,225-239
+  ST_FPD,   // A d: <Ad,q> -> c2                                   main.c:240-245
+  ST_PP,    // p = d + c2 p: nV, <p,d>, trace, k++                 main.c:247-251,148-162
+  ST_SQ,    // linear mode: q = Ad + c2 q: |q|^2 -> c1
+  ST_SA,    // linear mode: Af += c1 q, r -= c1 q: E_data
+  ST_E1,    // edge: d, nD, sum n d^2, nNablaD -> c                main.c:294-329
+  ST_E2,    // edge: v = clamp(v + c d): maxCD, exits              main.c:332-354
+};
+
+struct Ctl {
+  int enabled;      // scan takes part in launches at all
+  int img_active;   // image step running
+  int edge_active;  // edge step running
+  int k;            // inner iteration of the running step (1-based)
+  int outer;        // outer iteration (1-based)
+  int final_u;      // update buffer holding the image-step result (0 = F, 1 = U1)
+  int exit_reason;  // last exit: 1 maxIt, 2 tolerance, 3 instability
+  int trace_n;      // records written
+  unsigned arrive;  // CTA arrival counter of the current kernel
+  unsigned maxbits; // running max of a non-negative float (as bits)
+  int iter_image, iter_edge, median_every, mode;
+  double alpha, beta, eps;
+  double at_old, e_data, nv, pd, normap, c1, c2;
+  double nd, c;
+};
+
+constexpr int kTraceCap = 4096;  // records per scan (10 doubles each)
+
+struct ScanDev {
+  int kind, n, nviews, ndets;
+  int npix, nbins, nbpv, pad0;
+  // fan plan
+  const RayHdr *rays;
+  const uint32_t *bits;
+  const uint32_t *blk_word;
+  const uint8_t *blk_nw;
+  const float4 *view;
+  float det_inv_pitch, det_t0, pixel_mm, pad1;
+  // goldnc plan
+  const GcSeg *gc_seg;
+  const int32_t *gc_pair_off;
+  const GcEntry *gc_ent;
+  const int32_t *gc_pix_off;
+  // state
+  float *buf[B_NBUF];
+  Ctl *ctl;
+  double *partials;  // >= max CTAs of any kernel for this scan x 4 sums
+  double *trace;     // kTraceCap x 10
+};
+
+// One launch over the batch.  prefix[s]..prefix[s+1] are scan s's CTAs.
+struct Launch {
+  ScanDev single;        // used when scans == nullptr (plain projector calls)
+  const ScanDev *scans;
+  const int *prefix;
+  int nscans;
+  int flow;
+  int stage;
+  int in_buf, out_buf, aux_buf;  // buffer ids (meaning depends on the kernel)
+  int k;                         // inner iteration this launch belongs to
+  int flag;                      // kernel-specific (median this iteration, first pass, ...)
+};
+
+__device__ __forceinline__ int find_scan(const int *prefix, int nscans, int cta) {
+  int lo = 0, hi = nscans;  // prefix[lo] <= cta < prefix[hi]
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(prefix + mid) <= cta) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ const ScanDev &scan_of(const Launch &L, int s) {
+  return L.scans ? L.scans[s] : L.single;
+}
+
+__device__ __forceinline__ bool flow_active(const ScanDev &S, int flow) {
+  if (flow == FLOW_ALWAYS) return true;
+  const volatile Ctl *c = S.ctl;
+  if (!c->enabled) return false;
+  if (flow == FLOW_ENABLED) return true;
+  if (flow == FLOW_IMAGE) return c->img_active != 0;
+  return c->edge_active != 0;
+}
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ void trace_push(const ScanDev &S, int step, int k, int exit_reason, double s0, double s1,
+                                           double s2, double s3, double s4, double s5) {
+  Ctl *c = S.ctl;
+  const int i = c->trace_n;
+  if (i >= kTraceCap) return;
+  double *r = S.trace + (size_t)i * 10;
+  r[0] = c->outer;
+  r[1] = step;
+  r[2] = k;
+  r[3] = exit_reason;
+  r[4] = s0;
+  r[5] = s1;
+  r[6] = s2;
+  r[7] = s3;
+  r[8] = s4;
+  r[9] = s5;
+  c->trace_n = i + 1;
+}
+
+// Scalar part of a step, run by one thread of the last CTA.
+__device__ inline void finalize_stage(const ScanDev &S, const Launch &L, const double *s) {
+  Ctl *c = S.ctl;
+  const int k = L.k;
+  switch (L.stage) {
+    case ST_FP0:
+      c->e_data = s[0];
+      break;
+    case ST_BP0:
+      c->at_old = c->e_data + s[0];
+      break;
+    case ST_PP0:
+      c->nv = s[0];
+      c->pd = s[1];
+      break;
+    case ST_FPQ:
+    case ST_SQ:
+      c->normap = s[0];
+      c->c1 = c->pd / (c->normap + c->alpha * c->nv);  // main.c:167
+      break;
+    case ST_UPD: {
+      const float maxcp = __uint_as_float(c->maxbits);
+      c->maxbits = 0u;
+      const int next = (k & 1) ? 1 : 0;  // update buffer written at iteration k
+      if (k == c->iter_image) {          // main.c:184-187
+        trace_push(S, 0, k, 1, c->at_old, c->nv, c->pd, c->normap, c->c1, 0.0);
+        c->final_u = next;
+        c->exit_reason = 1;
+        c->img_active = 0;
+      } else if ((double)maxcp < 1e-5) {  // main.c:188-191
+        trace_push(S, 0, k, 2, c->at_old, c->nv, c->pd, c->normap, c->c1, 0.0);
+        c->final_u = next;
+        c->exit_reason = 2;
+        c->img_active = 0;
+      }
+      break;
+    }
+    case ST_FPA:
+    case ST_SA:
+      c->e_data = s[0];
+      break;
+    case ST_BPD: {
+      const double at_new = c->e_data + s[0];
+      if (1.1 * c->at_old < at_new && 1 < k) {  // main.c:209-215: keep the pre-step image
+        trace_push(S, 0, k, 3, c->at_old, c->nv, c->pd, c->normap, c->c1, 0.0);
+        c->final_u = (k & 1) ? 0 : 1;
+        c->exit_reason = 3;
+        c->img_active = 0;
+      } else {
+        c->at_old = at_new;
+      }
+      break;
+    }
+    case ST_FPD:
+      c->c2 = -s[0] / c->normap;  // main.c:245
+      break;
+    case ST_PP:
+      trace_push(S, 0, k, 0, c->at_old, c->nv, c->pd, c->normap, c->c1, c->c2);
+      c->nv = s[0];
+      c->pd = s[1];
+      c->k = k + 1;
+      break;
+    case ST_E1: {
+      const double nD = s[0], tmp = s[1], nNablaD = s[2];
+      c->nd = nD;
+      c->c = nD / (c->alpha * tmp + c->beta * c->eps * nNablaD + (c->beta / (4 * c->eps)) * nD);  // main.c:329
+      break;
+    }
+    case ST_E2: {
+      const float maxcd = __uint_as_float(c->maxbits);
+      c->maxbits = 0u;
+      if (k == c->iter_edge) {  // main.c:346-349
+        trace_push(S, 1, k, 1, c->nd, c->c, (double)maxcd, 0, 0, 0);
+        c->exit_reason = 1;
+        c->edge_active = 0;
+      } else if ((double)maxcd < 1e-5) {  // main.c:351-354
+        trace_push(S, 1, k, 2, c->nd, c->c, (double)maxcd, 0, 0, 0);
+        c->exit_reason = 2;
+        c->edge_active = 0;
+      } else {
+        trace_push(S, 1, k, 0, c->nd, c->c, (double)maxcd, 0, 0, 0);
+        c->k = k + 1;
+      }
+      break;
+    }
+    default:
+      break;
+  }
+}
+
+// Block-level reduction of NS FP64 values (blockDim.x a multiple of 32, <= 1024),
+// partial write, and the last-CTA finalize.  Must be reached by every thread
+// of the CTA.  `local_cta`/`ncta` index the CTA within its scan.
+template <int NS>
+__device__ void reduce_and_finalize(const ScanDev &S, const Launch &L, const double *v, int local_cta, int ncta) {
+  __shared__ double red[32][NS > 0 ? NS : 1];
+  __shared__ bool last;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (NS > 0) {
+#pragma unroll
+    for (int i = 0; i < NS; i++) {
+      const double w = warp_sum_d(v[i]);
+      if (lane == 0) red[warp][i] = w;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+      for (int i = 0; i < NS; i++) {
+        double a = 0;
+        for (int w = 0; w < nw; w++) a += red[w][i];
+        S.partials[(size_t)local_cta * NS + i] = a;
+      }
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned t = atomicAdd(&S.ctl->arrive, 1u);
+    last = (t == (unsigned)ncta - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  double acc[NS > 0 ? NS : 1];
+#pragma unroll
+  for (int i = 0; i < NS; i++) acc[i] = 0.0;
+  if (NS > 0) {
+    const volatile double *P = S.partials;
+    for (int c = threadIdx.x; c < ncta; c += blockDim.x)
+#pragma unroll
+      for (int i = 0; i < NS; i++) acc[i] += P[(size_t)c * NS + i];
+#pragma unroll
+    for (int i = 0; i < NS; i++) {
+      const double w = warp_sum_d(acc[i]);
+      if (lane == 0) red[warp][i] = w;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tot[NS > 0 ? NS : 1];
+#pragma unroll
+    for (int i = 0; i < NS; i++) {
+      double a = 0;
+      for (int w = 0; w < nw; w++) a += red[w][i];
+      tot[i] = a;
+    }
+    S.ctl->arrive = 0u;
+    finalize_stage(S, L, tot);
+    __threadfence();
+  }
+}
+
+__device__ __forceinline__ void atomic_max_nonneg(unsigned *addr, float x) {
+  atomicMax(addr, __float_as_uint(x));
+}
+
+}  // namespace at

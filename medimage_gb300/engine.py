@@ -1,0 +1,366 @@
+"""ctypes bindings of libat_engine.so (include/at_engine.h, include/goldnc.h)."""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libat_engine.so")
+
+AT_GEOM_GOLDNC, AT_GEOM_FAN = 0, 1
+_fp = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+
+
+class AtError(RuntimeError):
+    """A C-ABI call returned a negative status."""
+
+    def __init__(self, call: str, code: int, msg: str):
+        super().__init__(f"{call} failed ({code}): {msg}")
+        self.code = code
+
+
+class _FanGeom(C.Structure):
+    _fields_ = [
+        ("n", C.c_int32),
+        ("pixel_mm", C.c_double),
+        ("nviews", C.c_int32),
+        ("ndets", C.c_int32),
+        ("sod_mm", C.c_double),
+        ("sdd_mm", C.c_double),
+        ("det_pitch_deg", C.c_double),
+        ("off_center", C.c_double),
+        ("view0_deg", C.c_double),
+        ("view_step_deg", C.c_double),
+    ]
+
+
+class _Params(C.Structure):
+    _fields_ = [
+        ("alpha", C.c_double),
+        ("beta", C.c_double),
+        ("epsilon", C.c_double),
+        ("iter_alt", C.c_int32),
+        ("iter_image", C.c_int32),
+        ("iter_edge", C.c_int32),
+        ("mode", C.c_int32),
+    ]
+
+
+class _PlanStats(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int32),
+        ("n", C.c_int32),
+        ("nviews", C.c_int32),
+        ("ndets", C.c_int32),
+        ("rays", C.c_int64),
+        ("segments", C.c_int64),
+        ("offgrid", C.c_int64),
+        ("device_bytes", C.c_int64),
+        ("max_segments", C.c_int32),
+    ]
+
+
+# exported symbol -> (argtypes, restype); the table doubles as the ABI list the
+# CPU tests compare with include/*.h
+SIGNATURES = {
+    "at_last_error": ([], C.c_char_p),
+    "at_device_info": ([C.c_char_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_size_t)], C.c_int),
+    "at_plan_create_fan": ([C.POINTER(_FanGeom), C.POINTER(C.c_void_p)], C.c_int),
+    "at_plan_create_goldnc": ([C.POINTER(C.c_void_p)], C.c_int),
+    "at_plan_destroy": ([C.c_void_p], None),
+    "at_plan_get_stats": ([C.c_void_p, C.POINTER(_PlanStats)], C.c_int),
+    "at_plan_trace_ray": ([C.c_void_p, C.c_int32, C.c_int32, _ip, _fp, C.c_int32, C.POINTER(C.c_int32)], C.c_int),
+    "at_forward": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+    "at_back": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+    "at_forward_host": ([C.c_void_p, _fp, _fp], C.c_int),
+    "at_back_host": ([C.c_void_p, _fp, _fp], C.c_int),
+    "at_dev_alloc": ([C.POINTER(C.c_void_p), C.c_size_t], C.c_int),
+    "at_dev_free": ([C.c_void_p], C.c_int),
+    "at_memcpy_h2d": ([C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p], C.c_int),
+    "at_memcpy_d2h": ([C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p], C.c_int),
+    "at_stream_create": ([C.POINTER(C.c_void_p)], C.c_int),
+    "at_stream_destroy": ([C.c_void_p], C.c_int),
+    "at_stream_sync": ([C.c_void_p], C.c_int),
+    "at_solver_create": ([C.POINTER(C.c_void_p), C.c_int32, C.POINTER(_Params), C.POINTER(C.c_void_p)], C.c_int),
+    "at_solver_destroy": ([C.c_void_p], None),
+    "at_solver_footprint": ([C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_size_t)], C.c_int),
+    "at_solver_set_sino": ([C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p], C.c_int),
+    "at_solver_set_sino_host": ([C.c_void_p, C.c_int32, _fp, C.c_void_p], C.c_int),
+    "at_solver_reset": ([C.c_void_p, C.c_void_p], C.c_int),
+    "at_solver_run": ([C.c_void_p, C.c_void_p], C.c_int),
+    "at_solver_step": ([C.c_void_p, C.c_int32, C.c_void_p], C.c_int),
+    "at_solver_get": ([C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+    "at_solver_get_host": ([C.c_void_p, C.c_int32, _fp, _fp, C.c_void_p], C.c_int),
+    "at_solver_set_fv_host": ([C.c_void_p, C.c_int32, _fp, _fp, C.c_void_p], C.c_int),
+    "at_solver_trace": ([C.c_void_p, C.c_int32, _dp, C.c_int32, C.POINTER(C.c_int32)], C.c_int),
+    "at_solver_launches_per_outer": ([C.c_void_p, C.POINTER(C.c_int32)], C.c_int),
+    "at_reconstruct_host": ([C.c_void_p, C.POINTER(_Params), _fp, _fp, _fp], C.c_int),
+    # GoldenC drop-in (include/goldnc.h)
+    "A": ([_dp, _dp], None),
+    "AStar": ([_dp, _dp], None),
+    "minimize_in_IMAGE_variable": ([_dp, _dp, _dp, _dp, C.c_double, C.c_double, C.c_int], None),
+    "minimize_in_EDGE_variable": ([_dp, _dp, _dp, C.c_double, C.c_double, C.c_double, C.c_int], None),
+    "medfilt2": ([_dp], None),
+    "MumfordShah": ([C.c_double, C.c_double, C.c_double], None),
+    "goldnc_status": ([], C.c_int),
+    "goldnc_set_iterations": ([C.c_int, C.c_int, C.c_int], None),
+}
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Load libat_engine.so (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(
+                f"{LIB_PATH} is missing: build it with `python -m medimage_gb300.build` "
+                "(the engine has no CPU fallback)")
+        L = C.CDLL(LIB_PATH)
+        for name, (args, res) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        _lib = L
+    return _lib
+
+
+def _check(call: str, rc: int) -> None:
+    if rc != 0:
+        raise AtError(call, rc, lib().at_last_error().decode(errors="replace"))
+
+
+def device_info():
+    name = C.create_string_buffer(256)
+    sms = C.c_int()
+    mem = C.c_size_t()
+    _check("at_device_info", lib().at_device_info(name, 256, C.byref(sms), C.byref(mem)))
+    return {"name": name.value.decode(), "sm_count": sms.value, "hbm_bytes": mem.value}
+
+
+@dataclass
+class FanGeometry:
+    """2D fan-beam geometry with the parameters of the reference's fan tracer
+    (helical/rebin/src/main.h:16-47, ms2d.cpp:30-62,172-183)."""
+
+    n: int
+    pixel_mm: float
+    nviews: int
+    ndets: int
+    sod_mm: float = 541.0
+    sdd_mm: float = 949.0
+    det_pitch_deg: float = 0.0
+    off_center: float = 0.5
+    view0_deg: float = 0.0
+    view_step_deg: float = 0.0
+
+    @classmethod
+    def covering(cls, n: int, pixel_mm: float, nviews: int, ndets: int, sod_mm: float = 541.0,
+                 sdd_mm: float = 949.0, arc_deg: float = 360.0) -> "FanGeometry":
+        """Equiangular detector whose fan just covers the image's circumscribed
+        circle (fan = 2 asin(r / SOD), r = n * pixel * sqrt(2) / 2), views evenly
+        over `arc_deg`."""
+        r = n * pixel_mm * math.sqrt(2.0) / 2.0
+        fan_deg = 2.0 * math.degrees(math.asin(r / sod_mm))
+        return cls(n, pixel_mm, nviews, ndets, sod_mm, sdd_mm, fan_deg / ndets, 0.5, 0.0, arc_deg / nviews)
+
+    def c(self) -> _FanGeom:
+        return _FanGeom(self.n, self.pixel_mm, self.nviews, self.ndets, self.sod_mm, self.sdd_mm,
+                        self.det_pitch_deg, self.off_center, self.view0_deg, self.view_step_deg)
+
+
+@dataclass
+class Params:
+    """AT weights and iteration counts; defaults are GoldenC's config.h:6-17."""
+
+    alpha: float = 1000.0
+    beta: float = 0.002
+    epsilon: float = 0.0001
+    iter_alt: int = 10
+    iter_image: int = 10
+    iter_edge: int = 10
+    mode: int = 0  # 0 exact projection count, 1 linear-mode sinogram updates
+
+    def c(self) -> _Params:
+        return _Params(self.alpha, self.beta, self.epsilon, self.iter_alt, self.iter_image, self.iter_edge,
+                       self.mode)
+
+
+class Plan:
+    """Device-resident projector plan of one geometry."""
+
+    def __init__(self, handle: C.c_void_p, geom):
+        self._h = handle
+        self.geom = geom
+        st = _PlanStats()
+        _check("at_plan_get_stats", lib().at_plan_get_stats(self._h, C.byref(st)))
+        self.stats = {k: getattr(st, k) for k, _ in _PlanStats._fields_}
+        self.n, self.nviews, self.ndets = st.n, st.nviews, st.ndets
+
+    @classmethod
+    def fan(cls, geom: FanGeometry) -> "Plan":
+        h = C.c_void_p()
+        g = geom.c()
+        _check("at_plan_create_fan", lib().at_plan_create_fan(C.byref(g), C.byref(h)))
+        return cls(h, geom)
+
+    @classmethod
+    def goldnc(cls) -> "Plan":
+        h = C.c_void_p()
+        _check("at_plan_create_goldnc", lib().at_plan_create_goldnc(C.byref(h)))
+        return cls(h, None)
+
+    @property
+    def handle(self) -> C.c_void_p:
+        return self._h
+
+    def close(self) -> None:
+        if self._h:
+            lib().at_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def trace_ray(self, view: int, det: int):
+        cap = 4 * 8192
+        pix = np.zeros(cap, np.int32)
+        w = np.zeros(cap, np.float32)
+        n = C.c_int32()
+        _check("at_plan_trace_ray", lib().at_plan_trace_ray(self._h, view, det, pix, w, cap, C.byref(n)))
+        return pix[: n.value].copy(), w[: n.value].copy()
+
+    def forward(self, img: np.ndarray) -> np.ndarray:
+        img = np.ascontiguousarray(img, np.float32)
+        assert img.shape == (self.n, self.n)
+        out = np.zeros((self.nviews, self.ndets), np.float32)
+        _check("at_forward_host", lib().at_forward_host(self._h, img, out))
+        return out
+
+    def back(self, sino: np.ndarray) -> np.ndarray:
+        sino = np.ascontiguousarray(sino, np.float32)
+        assert sino.shape == (self.nviews, self.ndets)
+        out = np.zeros((self.n, self.n), np.float32)
+        _check("at_back_host", lib().at_back_host(self._h, sino, out))
+        return out
+
+    def forward_dev(self, d_img: int, d_sino: int, stream: int = 0) -> None:
+        _check("at_forward", lib().at_forward(self._h, C.c_void_p(d_img), C.c_void_p(d_sino), C.c_void_p(stream)))
+
+    def back_dev(self, d_sino: int, d_img: int, stream: int = 0) -> None:
+        _check("at_back", lib().at_back(self._h, C.c_void_p(d_sino), C.c_void_p(d_img), C.c_void_p(stream)))
+
+
+def _plan_array(plans):
+    arr = (C.c_void_p * len(plans))(*[p.handle for p in plans])
+    return arr
+
+
+class Solver:
+    """Batched AT solver over one or more plans (one scan per plan)."""
+
+    def __init__(self, plans, params: Params):
+        self.plans = list(plans)
+        self.params = params
+        self._h = C.c_void_p()
+        arr = _plan_array(self.plans)
+        prm = params.c()
+        _check("at_solver_create", lib().at_solver_create(arr, len(self.plans), C.byref(prm), C.byref(self._h)))
+
+    @staticmethod
+    def footprint(plans) -> int:
+        arr = _plan_array(list(plans))
+        b = C.c_size_t()
+        _check("at_solver_footprint", lib().at_solver_footprint(arr, len(plans), C.byref(b)))
+        return b.value
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if self._h:
+            lib().at_solver_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_sino(self, scan: int, sino: np.ndarray, stream: int = 0) -> None:
+        p = self.plans[scan]
+        sino = np.ascontiguousarray(sino, np.float32)
+        assert sino.shape == (p.nviews, p.ndets)
+        self._keep = sino  # host buffer must live until the copy completes
+        _check("at_solver_set_sino_host", lib().at_solver_set_sino_host(self._h, scan, sino, C.c_void_p(stream)))
+        self.sync(stream)
+
+    def set_sino_dev(self, scan: int, d_sino: int, stream: int = 0) -> None:
+        _check("at_solver_set_sino", lib().at_solver_set_sino(self._h, scan, C.c_void_p(d_sino), C.c_void_p(stream)))
+
+    def set_fv(self, scan: int, f: np.ndarray, v: np.ndarray, stream: int = 0) -> None:
+        f = np.ascontiguousarray(f, np.float32)
+        v = np.ascontiguousarray(v, np.float32)
+        _check("at_solver_set_fv_host", lib().at_solver_set_fv_host(self._h, scan, f, v, C.c_void_p(stream)))
+        self.sync(stream)
+
+    def reset(self, stream: int = 0) -> None:
+        _check("at_solver_reset", lib().at_solver_reset(self._h, C.c_void_p(stream)))
+
+    def run(self, stream: int = 0, sync: bool = True) -> None:
+        _check("at_solver_run", lib().at_solver_run(self._h, C.c_void_p(stream)))
+        if sync:
+            self.sync(stream)
+
+    def step(self, count: int, stream: int = 0, sync: bool = True) -> None:
+        _check("at_solver_step", lib().at_solver_step(self._h, count, C.c_void_p(stream)))
+        if sync:
+            self.sync(stream)
+
+    @staticmethod
+    def sync(stream: int = 0) -> None:
+        _check("at_stream_sync", lib().at_stream_sync(C.c_void_p(stream)))
+
+    def get(self, scan: int, stream: int = 0):
+        p = self.plans[scan]
+        f = np.zeros((p.n, p.n), np.float32)
+        v = np.zeros((p.n, p.n), np.float32)
+        _check("at_solver_get_host", lib().at_solver_get_host(self._h, scan, f, v, C.c_void_p(stream)))
+        return f, v
+
+    def trace(self, scan: int):
+        """Scalar trajectory: list of (outer, step, k, exit, s0..s5)."""
+        cap = 4096
+        buf = np.zeros(cap * 10, np.float64)
+        n = C.c_int32()
+        _check("at_solver_trace", lib().at_solver_trace(self._h, scan, buf, cap, C.byref(n)))
+        recs = buf[: 10 * n.value].reshape(-1, 10)
+        return [(int(r[0]), int(r[1]), int(r[2]), int(r[3]), tuple(float(x) for x in r[4:])) for r in recs]
+
+    @property
+    def launches_per_outer(self) -> int:
+        n = C.c_int32()
+        _check("at_solver_launches_per_outer", lib().at_solver_launches_per_outer(self._h, C.byref(n)))
+        return n.value
+
+
+def reconstruct(plan: Plan, params: Params, sino: np.ndarray):
+    """One call through at_reconstruct_host: host sinogram in, (f, v) out."""
+    sino = np.ascontiguousarray(sino, np.float32)
+    f = np.zeros((plan.n, plan.n), np.float32)
+    v = np.zeros((plan.n, plan.n), np.float32)
+    prm = params.c()
+    _check("at_reconstruct_host", lib().at_reconstruct_host(plan.handle, C.byref(prm), sino, f, v))
+    return f, v

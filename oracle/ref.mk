@@ -1,0 +1,40 @@
+# Compiles the reference's own sources for the hot path, straight from the
+# read-only reference tree, into oracle/_ref/ (git-ignored).  Used only to pin
+# the oracle restatement and to generate golden vectors.
+#
+#   make -f oracle/ref.mk REF=/root/reference
+#
+# Flags: -O2 without -ffast-math and with -ffp-contract=off, matching
+# oracle/Makefile, so that FP64 results can be compared bit for bit.  (The
+# reference's own Makefiles add -march=native -ffast-math, which lets the
+# compiler reassociate; those binaries are used for timing only.)
+REF ?= /root/reference
+HERE := $(dir $(abspath $(lastword $(MAKEFILE_LIST))))
+OUT := $(HERE)_ref
+CC ?= gcc
+CXX ?= g++
+FLAGS = -O2 -D_GNU_SOURCE -ffp-contract=off -fno-fast-math -fPIC
+GOLDNC := $(REF)/origin/GoldenC/src
+FANSRC := $(REF)/helical/rebin/src
+
+all: $(OUT)/libgoldnc_ref.so $(OUT)/libfan_ref.so $(OUT)/goldnc_fast
+
+$(OUT):
+	mkdir -p $(OUT)
+
+# GoldenC main.c + proj.c as a library; main() renamed so the solver entry
+# points (minimize_in_IMAGE_variable, ...) can be driven from tests.
+$(OUT)/libgoldnc_ref.so: $(GOLDNC)/main.c $(GOLDNC)/proj.c | $(OUT)
+	$(CC) $(FLAGS) -std=c99 -w -I$(GOLDNC) -Dmain=goldnc_ref_main -shared -o $@ $(GOLDNC)/main.c $(GOLDNC)/proj.c -lm
+
+# helical/rebin tracing.cpp with small stubs for the globals it reads.
+$(OUT)/libfan_ref.so: $(FANSRC)/tracing.cpp $(HERE)ref_shims/fan_ref_shim.cpp | $(OUT)
+	$(CXX) $(FLAGS) -std=c++14 -w -I$(FANSRC) -shared -o $@ $(FANSRC)/tracing.cpp $(HERE)ref_shims/fan_ref_shim.cpp -lm
+
+# GoldenC with the reference's own optimisation flags (timing comparator only).
+$(OUT)/goldnc_fast: $(GOLDNC)/main.c $(GOLDNC)/proj.c | $(OUT)
+	$(CC) -O3 -std=c99 -D_GNU_SOURCE -w -funroll-all-loops -ffast-math -I$(GOLDNC) -Dmain=goldnc_ref_main -shared -fPIC -o $(OUT)/libgoldnc_fast.so $(GOLDNC)/main.c $(GOLDNC)/proj.c -lm && touch $@
+
+clean:
+	rm -rf $(OUT)
+.PHONY: all clean

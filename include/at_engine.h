@@ -90,6 +90,8 @@ typedef struct at_plan_stats {
     int64_t offgrid;       /* segments the reference traces off the pixel grid */
     int64_t device_bytes;  /* plan memory in HBM                               */
     int32_t max_segments;  /* longest ray                                      */
+    int32_t fp_rays_per_thread; /* forward-projector variant the autotuner chose */
+    int64_t bp_runs;       /* (ray, 16x16 tile) runs the back projector walks   */
 } at_plan_stats;
 
 const char *at_last_error(void);

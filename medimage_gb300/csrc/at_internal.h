@@ -25,6 +25,7 @@
 namespace at {
 
 constexpr int kRayBlock = 128;  // rays per decision-bit block (one view)
+constexpr int kBpTile = 16;     // back-projection tile edge (pixels)
 
 // Per-ray header.  Boundary parameters are relative to the ray's entry
 // lambda_min (mm): the k-th x-plane crossing is at fmaf(k, lenx, ax), the k-th
@@ -54,15 +55,20 @@ struct Plan {
   int n = 0, nviews = 0, ndets = 0;
   int64_t rays = 0, segments = 0, offgrid = 0, device_bytes = 0;
   int max_segments = 0;
+  int fp_rpt = 1;  // rays per thread of the forward projector (autotuned)
   // fan
   RayHdr *rays_d = nullptr;
   uint32_t *bits_d = nullptr;
   uint32_t *blk_word_d = nullptr;
   uint8_t *blk_nw_d = nullptr;
   int nblocks_per_view = 0, nblocks = 0;
-  float4 *view_d = nullptr;  // per view: {sx, sy, cos(beta), sin(beta)} (mm, FP32)
-  float det_inv_pitch = 0.f; // 1/detector pitch (rad^-1)
-  float det_t0 = 0.f;        // ndets/2 - off_center
+  // back projection: one entry per (ray, 16x16 tile) run of the traversal,
+  // grouped by tile, longest runs first.  Entry = {ray, k_in | nk << 16,
+  // cx_in | prev_step_was_x << 16, tile-local x | y << 4 | signx << 8 | signy << 9}
+  uint4 *run_d = nullptr;
+  int32_t *tile_off_d = nullptr;  // [ntiles + 1]
+  int ntiles_y = 0, ntiles = 0;
+  int64_t nruns = 0;
   // goldnc
   GcSeg *gc_seg_d = nullptr;
   int32_t *gc_pair_off_d = nullptr;  // [17280+1]
@@ -87,6 +93,7 @@ int validate_fan(const at_fan_geometry &g);
 // plan construction (plan.cu)
 int build_fan_plan(Plan &p, cudaStream_t st);
 int build_goldnc_plan(Plan &p, cudaStream_t st);
+int autotune_fan(Plan &p, cudaStream_t st);
 
 }  // namespace at
 

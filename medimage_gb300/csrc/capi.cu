@@ -116,6 +116,7 @@ AT_API int at_plan_create_fan(const at_fan_geometry *geom, at_plan **out) {
   cudaStream_t st;
   AT_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
   rc = build_fan_plan(P->p, st);
+  if (!rc) rc = autotune_fan(P->p, st);
   cudaStreamSynchronize(st);
   cudaStreamDestroy(st);
   if (rc) return rc;
@@ -156,6 +157,8 @@ AT_API int at_plan_get_stats(const at_plan *plan, at_plan_stats *out) {
   out->offgrid = p.offgrid;
   out->device_bytes = p.device_bytes;
   out->max_segments = p.max_segments;
+  out->fp_rays_per_thread = p.fp_rpt;
+  out->bp_runs = p.nruns;
   return AT_OK;
 }
 

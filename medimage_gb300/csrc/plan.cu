@@ -13,6 +13,8 @@
 #include <cstring>
 #include <vector>
 
+#include <cub/device/device_radix_sort.cuh>
+
 #include "at_internal.h"
 
 namespace at {
@@ -158,6 +160,137 @@ int dev_alloc(T **p, size_t count, int64_t &acct) {
 }
 }  // namespace
 
+// ---------------------------------------------------------------------------
+// back-projection runs: the traversal of every ray cut into its runs through
+// 16x16 pixel tiles, so the back projector can own a tile and walk exactly the
+// forward projector's segments inside it.
+// ---------------------------------------------------------------------------
+template <int kMode>
+__global__ void fan_runs_kernel(int n, int nviews, int ndets, int nbpv, const RayHdr *hdr, const uint32_t *bits,
+                                const uint32_t *blk_word, int tiles_y, int *tile_count, unsigned long long *cursor,
+                                uint4 *ent, unsigned long long *keys) {
+  const int ray = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ray >= nviews * ndets) return;
+  const RayHdr h = hdr[ray];
+  if (h.nseg == 0) return;
+  const int view = ray / ndets, det = ray % ndets;
+  const uint32_t *wp = bits + blk_word[view * nbpv + det / kRayBlock] + (det % kRayBlock);
+  int x = h.xy0 & 0xffff, y = h.xy0 >> 16;
+  const int sx = (h.sgn & 1) ? 1 : -1, sy = (h.sgn & 2) ? 1 : -1;
+  int cx = 0, cur_tile = -1, run_k = 0, run_cx = 0, run_prevx = 0, run_lx = 0, run_ly = 0, last_bit = 0;
+  uint32_t word = 0;
+  auto close_run = [&](int k_end) {
+    if (cur_tile < 0) return;
+    const int nk = k_end - run_k;
+    if (kMode == 0) {
+      atomicAdd(&tile_count[cur_tile], 1);
+    } else {
+      const unsigned long long pos = atomicAdd(cursor, 1ull);
+      ent[pos] = make_uint4((unsigned)ray, (unsigned)run_k | ((unsigned)nk << 16),
+                            (unsigned)run_cx | ((unsigned)run_prevx << 16),
+                            (unsigned)run_lx | ((unsigned)run_ly << 4) | ((h.sgn & 1u) << 8) | (((h.sgn >> 1) & 1u) << 9));
+      keys[pos] = ((unsigned long long)cur_tile << 38) | ((unsigned long long)(63 - nk) << 32) | (unsigned)ray;
+    }
+  };
+  for (int k = 0; k < h.nseg; k++) {
+    if ((k & 31) == 0) word = wp[(size_t)(k >> 5) * kRayBlock];
+    const bool inside = (unsigned)x < (unsigned)n && (unsigned)y < (unsigned)n;
+    const int t = inside ? (x >> 4) * tiles_y + (y >> 4) : -1;
+    if (t != cur_tile) {
+      close_run(k);
+      cur_tile = t;
+      run_k = k;
+      run_cx = cx;
+      run_prevx = last_bit;
+      run_lx = x & 15;
+      run_ly = y & 15;
+    }
+    const int bit = (word >> (k & 31)) & 1;
+    if (bit) {
+      x += sx;
+      cx++;
+    } else {
+      y += sy;
+    }
+    last_bit = bit;
+  }
+  close_run(h.nseg);
+}
+
+__global__ void gather_runs_kernel(const uint4 *src, const unsigned *idx, uint4 *dst, int64_t count) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < count) dst[i] = src[idx[i]];
+}
+
+__global__ void iota_kernel(unsigned *v, int64_t count) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < count) v[i] = (unsigned)i;
+}
+
+int build_fan_runs(Plan &p, cudaStream_t st) {
+  const int nrays = p.nviews * p.ndets, tpb = 128;
+  p.ntiles_y = (p.n + kBpTile - 1) / kBpTile;
+  p.ntiles = p.ntiles_y * p.ntiles_y;
+  int *cnt_d = nullptr;
+  unsigned long long *cur_d = nullptr;
+  AT_CUDA_TRY(cudaMalloc(&cnt_d, sizeof(int) * p.ntiles));
+  AT_CUDA_TRY(cudaMalloc(&cur_d, sizeof(unsigned long long)));
+  AT_CUDA_TRY(cudaMemsetAsync(cnt_d, 0, sizeof(int) * p.ntiles, st));
+  AT_CUDA_TRY(cudaMemsetAsync(cur_d, 0, sizeof(unsigned long long), st));
+  fan_runs_kernel<0><<<(nrays + tpb - 1) / tpb, tpb, 0, st>>>(p.n, p.nviews, p.ndets, p.nblocks_per_view, p.rays_d,
+                                                              p.bits_d, p.blk_word_d, p.ntiles_y, cnt_d, nullptr,
+                                                              nullptr, nullptr);
+  AT_CUDA_TRY(cudaGetLastError());
+  std::vector<int> cnt(p.ntiles);
+  AT_CUDA_TRY(cudaMemcpyAsync(cnt.data(), cnt_d, sizeof(int) * p.ntiles, cudaMemcpyDeviceToHost, st));
+  AT_CUDA_TRY(cudaStreamSynchronize(st));
+  std::vector<int32_t> off(p.ntiles + 1);
+  int64_t tot = 0;
+  for (int t = 0; t < p.ntiles; t++) {
+    off[t] = (int32_t)tot;
+    tot += cnt[t];
+  }
+  if (tot >= (1ll << 31)) return set_error(AT_EINVAL, "plan: too many back-projection runs");
+  off[p.ntiles] = (int32_t)tot;
+  p.nruns = tot;
+  uint4 *tmp_ent = nullptr;
+  unsigned long long *keys = nullptr, *keys_out = nullptr;
+  unsigned *idx = nullptr, *idx_out = nullptr;
+  AT_CUDA_TRY(cudaMalloc(&tmp_ent, sizeof(uint4) * std::max<int64_t>(tot, 1)));
+  AT_CUDA_TRY(cudaMalloc(&keys, sizeof(unsigned long long) * std::max<int64_t>(tot, 1)));
+  AT_CUDA_TRY(cudaMalloc(&keys_out, sizeof(unsigned long long) * std::max<int64_t>(tot, 1)));
+  AT_CUDA_TRY(cudaMalloc(&idx, sizeof(unsigned) * std::max<int64_t>(tot, 1)));
+  AT_CUDA_TRY(cudaMalloc(&idx_out, sizeof(unsigned) * std::max<int64_t>(tot, 1)));
+  fan_runs_kernel<1><<<(nrays + tpb - 1) / tpb, tpb, 0, st>>>(p.n, p.nviews, p.ndets, p.nblocks_per_view, p.rays_d,
+                                                              p.bits_d, p.blk_word_d, p.ntiles_y, nullptr, cur_d,
+                                                              tmp_ent, keys);
+  AT_CUDA_TRY(cudaGetLastError());
+  iota_kernel<<<(int)((tot + 255) / 256) + 1, 256, 0, st>>>(idx, tot);
+  AT_CUDA_TRY(cudaGetLastError());
+  // keys are unique (tile, 63-nk, ray): the sorted order is deterministic
+  size_t temp_bytes = 0;
+  AT_CUDA_TRY(cub::DeviceRadixSort::SortPairs(nullptr, temp_bytes, keys, keys_out, idx, idx_out, (int64_t)tot, 0, 64, st));
+  void *temp = nullptr;
+  AT_CUDA_TRY(cudaMalloc(&temp, std::max<size_t>(temp_bytes, 1)));
+  AT_CUDA_TRY(cub::DeviceRadixSort::SortPairs(temp, temp_bytes, keys, keys_out, idx, idx_out, (int64_t)tot, 0, 64, st));
+  int rc;
+  if ((rc = dev_alloc(&p.run_d, tot, p.device_bytes))) return rc;
+  if ((rc = dev_alloc(&p.tile_off_d, p.ntiles + 1, p.device_bytes))) return rc;
+  gather_runs_kernel<<<(int)((tot + 255) / 256) + 1, 256, 0, st>>>(tmp_ent, idx_out, p.run_d, tot);
+  AT_CUDA_TRY(cudaGetLastError());
+  AT_CUDA_TRY(cudaMemcpyAsync(p.tile_off_d, off.data(), sizeof(int32_t) * (p.ntiles + 1), cudaMemcpyHostToDevice, st));
+  AT_CUDA_TRY(cudaStreamSynchronize(st));
+  cudaFree(temp);
+  cudaFree(tmp_ent);
+  cudaFree(keys);
+  cudaFree(keys_out);
+  cudaFree(idx);
+  cudaFree(idx_out);
+  cudaFree(cnt_d);
+  cudaFree(cur_d);
+  return AT_OK;
+}
+
 int build_fan_plan(Plan &p, cudaStream_t st) {
   const at_fan_geometry &g = p.geom;
   const int nv = g.nviews, nd = g.ndets, nrays = nv * nd;
@@ -230,19 +363,7 @@ int build_fan_plan(Plan &p, cudaStream_t st) {
   fan_fill_kernel<<<(nrays + tpb - 1) / tpb, tpb, 0, st>>>(g, T, p.nblocks_per_view, p.blk_word_d, p.bits_d);
   AT_CUDA_TRY(cudaGetLastError());
 
-  // per-view source position and central direction for the back projector
-  std::vector<float4> views(nv);
-  for (int v = 0; v < nv; v++) {
-    const double sx = g.sod_mm * scos[v] + g.n * g.pixel_mm / 2.0;
-    const double sy = g.sod_mm * ssin[v] + g.n * g.pixel_mm / 2.0;
-    views[v] = make_float4((float)sx, (float)sy, (float)scos[v], (float)ssin[v]);
-  }
-  if ((rc = dev_alloc(&p.view_d, nv, p.device_bytes))) return rc;
-  AT_CUDA_TRY(cudaMemcpyAsync(p.view_d, views.data(), sizeof(float4) * nv, cudaMemcpyHostToDevice, st));
-  const double pitch_rad = g.det_pitch_deg * M_PI / 180.;
-  p.det_inv_pitch = (float)(1.0 / pitch_rad);
-  p.det_t0 = (float)(nd / 2 - g.off_center);
-  p.device_bytes += (int64_t)sizeof(RayHdr) * 0;  // headers already counted
+  if ((rc = build_fan_runs(p, st))) return rc;
   AT_CUDA_TRY(cudaStreamSynchronize(st));
   cudaFree(tab_d);
   return AT_OK;
@@ -473,7 +594,8 @@ Plan::~Plan() {
   cudaFree(bits_d);
   cudaFree(blk_word_d);
   cudaFree(blk_nw_d);
-  cudaFree(view_d);
+  cudaFree(run_d);
+  cudaFree(tile_off_d);
   cudaFree(gc_seg_d);
   cudaFree(gc_pair_off_d);
   cudaFree(gc_ent_d);

@@ -8,17 +8,19 @@
 // into a Kahan-compensated total.  The traversal (pixel sequence) is the
 // reference's FP64 one (helical/rebin/src/tracing.cpp:118-146); weights are
 // differences of FP32 boundary crossings.
-// Fan beam, back: one thread per pixel gathers, view by view, the few rays
-// whose plan passes through the pixel, with the same FP32 crossing formula the
-// forward walk uses, so A^T is the transpose of A up to FP32 rounding, and no
-// atomics are involved (deterministic).
+// Fan beam, back: one CTA per 16x16 pixel tile walks the plan's (ray, tile)
+// runs with the forward walk's bits and crossing formula (so A^T is the exact
+// transpose of the FP32 A), accumulating in 64-bit fixed point in shared
+// memory: integer sums do not depend on arrival order (deterministic).
 // GoldenC: forward = one warp per traced (alpha, raynum) pair summing its 16
 // tile walks into the 8 symmetric bins of proj.c:114-127; back = one thread
 // per pixel over the transposed walk lists, with the 90-degree column of
 // proj.c:225.
 #include <cuda_runtime.h>
 
-#include "solver_dev.cuh"
+#include <cstring>
+
+#include "solver.h"
 
 namespace at {
 
@@ -192,8 +194,11 @@ __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
           cy[r] += bx ? 0.f : 1.f;
         }
       }
+      // fold only words that hold segments of this ray, so the result does not
+      // depend on how many rays share the warp's trip count
 #pragma unroll
-      for (int r = 0; r < RPT; r++) kahan_add(acc[r], comp[r], part[r]);
+      for (int r = 0; r < RPT; r++)
+        if (base < nseg[r]) kahan_add(acc[r], comp[r], part[r]);
     }
     const int row0 = view * S.ndets;
 #pragma unroll
@@ -209,63 +214,109 @@ __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
 }
 
 // ---------------------------------------------------------------------------
-// fan-beam back projection (gather)
+// fan-beam back projection (gather over tile runs)
 // ---------------------------------------------------------------------------
-// CTA = 8 x 32 pixel tile (x rows by y columns), one pixel per thread.
+// CTA = one 16x16 pixel tile, 256 threads.  The plan lists every (ray, tile)
+// run of the traversal that crosses the tile, longest first; warps take 32
+// runs at a time and walk them with the forward walk's decision bits and
+// crossing formula, so each segment gets the forward projector's weight
+// bit-for-bit.  Each contribution w*r is scaled to a 31-bit integer (a power
+// of two chosen per tile from the largest |r| on its runs) and split into its
+// high part (>> 15) and low 15 bits, accumulated in two 32-bit shared-memory
+// integer accumulators; integer addition is associative, so the result does
+// not depend on the order in which lanes, warps or views arrive
+// (deterministic, no float atomics), and neither accumulator can overflow for
+// fewer than 32768 contributions per pixel.
+constexpr int kBpPitch = kBpTile + 1;  // padded row pitch of the accumulator
+
 __global__ void __launch_bounds__(256) fan_bp_kernel(const Launch L) {
   const int scan = L.scans ? find_scan(L.prefix, L.nscans, blockIdx.x) : 0;
   const ScanDev &S = scan_of(L, scan);
   if (!flow_active(S, L.flow)) return;
   const int cta0 = L.scans ? __ldg(L.prefix + scan) : 0;
   const int ncta = L.scans ? __ldg(L.prefix + scan + 1) - cta0 : gridDim.x;
-  const int local_cta = blockIdx.x - cta0;
-  const int n = S.n;
-  const int tiles_y = (n + 31) >> 5;
-  const int x = (local_cta / tiles_y) * 8 + (threadIdx.x >> 5);
-  const int y = (local_cta % tiles_y) * 32 + (threadIdx.x & 31);
-  const bool inside = x < n && y < n;
+  const int tile = blockIdx.x - cta0;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __shared__ int acc_hi[kBpTile * kBpPitch], acc_lo[kBpTile * kBpPitch];
+  __shared__ float wmax[8];
+  for (int i = threadIdx.x; i < kBpTile * kBpPitch; i += blockDim.x) {
+    acc_hi[i] = 0;
+    acc_lo[i] = 0;
+  }
   const float *__restrict__ sino = S.buf[L.in_buf];
-  const float px = S.pixel_mm;
-  const float Px = (x + 0.5f) * px, Py = (y + 0.5f) * px;
-  const float half = 0.5f * px, diag = 0.70711f * px;
-  float acc = 0.f, comp = 0.f;
-  if (inside) {
-    for (int view = 0; view < S.nviews; view++) {
-      const float4 vw = __ldg(S.view + view);  // sx, sy, cos(beta), sin(beta)
-      const float Dx = Px - vw.x, Dy = Py - vw.y;
-      const float along = -(Dx * vw.z + Dy * vw.w);
-      const float perp = Dx * vw.w - Dy * vw.z;
-      const float t = atanf(perp / along) * S.det_inv_pitch + S.det_t0;
-      const float dist = sqrtf(along * along + perp * perp);
-      const float h = half * (fabsf(Dx) + fabsf(Dy)) / dist / (dist - diag) * S.det_inv_pitch + 1e-3f;
-      const int jlo = max(0, (int)ceilf(t - h));
-      const int jhi = min(S.ndets - 1, (int)floorf(t + h));
-      float contrib = 0.f;
-      for (int j = jlo; j <= jhi; j++) {
-        const uint4 *hp = reinterpret_cast<const uint4 *>(S.rays + (size_t)view * S.ndets + j);
-        const uint4 h0 = __ldg(hp);
-        const int x0 = (int)(h0.z & 0xffffu), y0 = (int)(h0.z >> 16);
-        const int cx = (h0.w & 1u) ? x - x0 : x0 - x;
-        const int cy = (h0.w & 2u) ? y - y0 : y0 - y;
-        if (cx < 0 || cy < 0 || cx + cy >= (int)h0.y) continue;
-        const uint4 h1 = __ldg(hp + 1);
-        const float ax = __uint_as_float(h1.x), ay = __uint_as_float(h1.y);
-        const float lx = __uint_as_float(h1.z), ly = __uint_as_float(h1.w);
-        const float fcx = (float)cx, fcy = (float)cy;
-        const float ex = fmaf(fcx, lx, ax), ey = fmaf(fcy, ly, ay);
-        const float ix = cx > 0 ? fmaf(fcx - 1.f, lx, ax) : 0.f;
-        const float iy = cy > 0 ? fmaf(fcy - 1.f, ly, ay) : 0.f;
-        const float wt = fminf(ex, ey) - fmaxf(ix, iy);
-        if (wt > 0.f) contrib = fmaf(wt, __ldg(sino + (size_t)view * S.ndets + j), contrib);
+  const int e0 = __ldg(S.tile_off + tile), e1 = __ldg(S.tile_off + tile + 1);
+  // fixed-point scale from the largest |r| on the tile's runs
+  float m = 0.f;
+  for (int i = e0 + threadIdx.x; i < e1; i += blockDim.x) m = fmaxf(m, fabsf(__ldg(sino + __ldg(&S.run[i].x))));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if (lane == 0) wmax[warp] = m;
+  __syncthreads();
+  m = wmax[0];
+  for (int w = 1; w < (int)(blockDim.x >> 5); w++) m = fmaxf(m, wmax[w]);
+  // every |w r| <= 1.5 * pixel * m < 2^ex; terms are scaled below 2^30
+  int ex = 0;
+  frexpf(fmaxf(1.5f * S.pixel_mm * m, 1e-30f), &ex);
+  const int sexp = min(30 - ex, 120);
+  const float scale = ldexpf(1.f, sexp);
+  if (m > 0.f) {
+    for (int c = e0 + warp * 32; c < e1; c += blockDim.x) {
+      const int i = c + lane;
+      const bool valid = i < e1;
+      const uint4 e = valid ? __ldg(S.run + i) : make_uint4(0u, 0u, 0u, 0u);
+      const int nk = (int)(e.y >> 16);
+      const int ray = (int)e.x;
+      const int k_in = (int)(e.y & 0xffffu), cx_in = (int)(e.z & 0xffffu);
+      const int view = ray / S.ndets, det = ray - view * S.ndets;
+      const uint4 h1 = __ldg(reinterpret_cast<const uint4 *>(S.rays + ray) + 1);
+      const float ax = __uint_as_float(h1.x), ay = __uint_as_float(h1.y);
+      const float lx = __uint_as_float(h1.z), ly = __uint_as_float(h1.w);
+      const int blk = view * S.nbpv + (det >> 7);
+      const uint32_t *wp = S.bits + __ldg(S.blk_word + blk) + (det & (kRayBlock - 1));
+      const int wi = k_in >> 5;
+      uint32_t w0 = 0u, w1 = 0u;
+      if (valid) {
+        w0 = __ldg(wp + (size_t)wi * kRayBlock);
+        if (wi + 1 < (int)__ldg(S.blk_nw + blk)) w1 = __ldg(wp + (size_t)(wi + 1) * kRayBlock);
       }
-      kahan_add(acc, comp, contrib);
+      const uint32_t wnd = __funnelshift_r(w0, w1, k_in & 31);
+      const float rs = valid ? __ldg(sino + ray) * scale : 0.f;
+      float cxf = (float)cx_in, cyf = (float)(k_in - cx_in);
+      float prev = 0.f;
+      if (k_in > 0) prev = ((e.z >> 16) & 1u) ? fmaf(cxf - 1.f, lx, ax) : fmaf(cyf - 1.f, ly, ay);
+      int sidx = (int)(e.w & 15u) * kBpPitch + (int)((e.w >> 4) & 15u);
+      const int dsx = (e.w & 256u) ? kBpPitch : -kBpPitch, dsy = (e.w & 512u) ? 1 : -1;
+      const int steps = (int)__reduce_max_sync(0xffffffffu, (unsigned)nk);
+      for (int t = 0; t < steps; t++) {
+        const bool bx = (wnd >> t) & 1u;
+        const float nx = fmaf(cxf, lx, ax), ny = fmaf(cyf, ly, ay);
+        const float cur = bx ? nx : ny;
+        const float wt = cur - prev;
+        prev = cur;
+        if (t < nk) {
+          const int q = __float2int_rn(wt * rs);
+          atomicAdd(&acc_hi[sidx], q >> 15);
+          atomicAdd(&acc_lo[sidx], q & 0x7fff);
+        }
+        sidx += bx ? dsx : dsy;
+        cxf += bx ? 1.f : 0.f;
+        cyf += bx ? 0.f : 1.f;
+      }
     }
   }
+  __syncthreads();
+  const int x = (tile / S.ntiles_y) * kBpTile + (threadIdx.x >> 4);
+  const int y = (tile % S.ntiles_y) * kBpTile + (threadIdx.x & 15);
   double s0 = 0.0;
-  if (inside) bp_epilogue(S, L, x, y, acc - comp, s0);
+  if (x < S.n && y < S.n) {
+    const int j = (threadIdx.x >> 4) * kBpPitch + (threadIdx.x & 15);
+    const long long a = (long long)acc_hi[j] * 32768ll + (long long)acc_lo[j];
+    const float val = (float)((double)a * ldexp(1.0, -sexp));
+    bp_epilogue(S, L, x, y, val, s0);
+  }
   if (stage_reduces(L.stage)) {
     double v[1] = {s0};
-    reduce_and_finalize<1>(S, L, v, local_cta, ncta);
+    reduce_and_finalize<1>(S, L, v, tile, ncta);
   }
 }
 
@@ -414,8 +465,10 @@ int fp_ctas(const ScanDev &S, int rpt) {
 
 int bp_ctas(const ScanDev &S) {
   if (S.kind == AT_GEOM_GOLDNC) return (kGcN / 8) * (kGcN / 32);
-  return ((S.n + 7) / 8) * ((S.n + 31) / 32);
+  return S.ntiles_y * S.ntiles_y;
 }
+
+int pix_ctas(const ScanDev &S) { return ((S.n + 7) / 8) * ((S.n + 31) / 32); }
 
 cudaError_t launch_fp(const Launch &L, int kind, int rpt, int nctas, cudaStream_t st) {
   if (kind == AT_GEOM_GOLDNC) {
@@ -434,6 +487,57 @@ cudaError_t launch_bp(const Launch &L, int kind, int nctas, cudaStream_t st) {
   if (kind == AT_GEOM_GOLDNC) gc_bp_kernel<<<nctas, 256, 0, st>>>(L);
   else fan_bp_kernel<<<nctas, 256, 0, st>>>(L);
   return cudaGetLastError();
+}
+
+}  // namespace at
+
+namespace at {
+
+// Times the forward projector with 1, 2 and 4 rays per thread on this plan and
+// keeps the fastest (results are bitwise identical across the three).
+int autotune_fan(Plan &p, cudaStream_t st) {
+  p.fp_rpt = 1;
+  if (p.kind != AT_GEOM_FAN) return AT_OK;
+  float *img = nullptr, *sino = nullptr;
+  const size_t npix = (size_t)p.n * p.n, nbins = (size_t)p.nviews * p.ndets;
+  AT_CUDA_TRY(cudaMallocAsync(&img, npix * sizeof(float), st));
+  AT_CUDA_TRY(cudaMallocAsync(&sino, nbins * sizeof(float), st));
+  AT_CUDA_TRY(cudaMemsetAsync(img, 0, npix * sizeof(float), st));
+  Launch L;
+  memset(&L, 0, sizeof(L));
+  fill_scan_plan(L.single, p);
+  L.single.buf[0] = img;
+  L.single.buf[1] = sino;
+  L.nscans = 1;
+  L.flow = FLOW_ALWAYS;
+  L.stage = ST_NONE;
+  L.in_buf = 0;
+  L.out_buf = 1;
+  L.aux_buf = -1;
+  cudaEvent_t e0, e1;
+  AT_CUDA_TRY(cudaEventCreate(&e0));
+  AT_CUDA_TRY(cudaEventCreate(&e1));
+  float best = 1e30f;
+  const int cands[3] = {1, 2, 4};
+  for (int rpt : cands) {
+    AT_CUDA_TRY(launch_fp(L, p.kind, rpt, fp_ctas(L.single, rpt), st));
+    AT_CUDA_TRY(cudaEventRecord(e0, st));
+    for (int i = 0; i < 3; i++) AT_CUDA_TRY(launch_fp(L, p.kind, rpt, fp_ctas(L.single, rpt), st));
+    AT_CUDA_TRY(cudaEventRecord(e1, st));
+    AT_CUDA_TRY(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    AT_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+    if (ms < best) {
+      best = ms;
+      p.fp_rpt = rpt;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFreeAsync(img, st);
+  cudaFreeAsync(sino, st);
+  AT_CUDA_TRY(cudaStreamSynchronize(st));
+  return AT_OK;
 }
 
 }  // namespace at

@@ -17,6 +17,7 @@ namespace at {
 
 int fp_ctas(const ScanDev &S, int rpt);
 int bp_ctas(const ScanDev &S);
+int pix_ctas(const ScanDev &S);
 cudaError_t launch_fp(const Launch &L, int kind, int rpt, int nctas, cudaStream_t st);
 cudaError_t launch_bp(const Launch &L, int kind, int nctas, cudaStream_t st);
 cudaError_t launch_pixel(int which, const Launch &L, int nctas, cudaStream_t st);
@@ -35,9 +36,9 @@ void fill_scan_plan(ScanDev &S, const Plan &p) {
   S.bits = p.bits_d;
   S.blk_word = p.blk_word_d;
   S.blk_nw = p.blk_nw_d;
-  S.view = p.view_d;
-  S.det_inv_pitch = p.det_inv_pitch;
-  S.det_t0 = p.det_t0;
+  S.run = p.run_d;
+  S.tile_off = p.tile_off_d;
+  S.ntiles_y = p.ntiles_y;
   S.pixel_mm = (float)p.geom.pixel_mm;
   S.gc_seg = p.gc_seg_d;
   S.gc_pair_off = p.gc_pair_off_d;
@@ -64,7 +65,8 @@ ScanLayout layout_of(const Plan &p, int rpt) {
   tmp.n = p.n;
   tmp.nviews = p.nviews;
   tmp.nbpv = p.nblocks_per_view;
-  const int maxcta = std::max({fp_ctas(tmp, rpt), bp_ctas(tmp), (int)((nbins + 255) / 256)});
+  tmp.ntiles_y = p.ntiles_y;
+  const int maxcta = std::max({fp_ctas(tmp, rpt), bp_ctas(tmp), pix_ctas(tmp), (int)((nbins + 255) / 256)});
   L.partial_bytes = align_up((size_t)maxcta * 4 * sizeof(double));
   L.trace_bytes = align_up((size_t)kTraceCap * 10 * sizeof(double));
   L.total = L.img_bytes * B_NIMG + L.sino_bytes * (B_NBUF - B_NIMG) + L.partial_bytes + L.trace_bytes +
@@ -74,10 +76,9 @@ ScanLayout layout_of(const Plan &p, int rpt) {
 }  // namespace
 
 int Solver::choose_rpt(const std::vector<Plan *> &plans) {
-  // rays per thread of the forward projector; one value for every batch so a
-  // scan's results do not depend on what it is batched with
-  (void)plans;
-  return 1;
+  // rays per thread of the forward projector: the autotuned choice of the
+  // batch's first plan (projections are bitwise identical for every choice)
+  return plans.empty() ? 1 : plans[0]->fp_rpt;
 }
 
 size_t Solver::footprint(const std::vector<Plan *> &plans, int rpt) {
@@ -114,7 +115,8 @@ int Solver::create(const std::vector<Plan *> &pl, const at_params &prm) {
   AT_CUDA_TRY(cudaMemset(arena, 0, total));
   host_scans.resize(nscans);
   char *cur = (char *)arena;
-  std::vector<int> fp_pref(nscans + 1, 0), bp_pref(nscans + 1, 0), sino_pref(nscans + 1, 0);
+  std::vector<int> fp_pref(nscans + 1, 0), pix_pref(nscans + 1, 0), sino_pref(nscans + 1, 0),
+      bp_pref(nscans + 1, 0);
   for (int s = 0; s < nscans; s++) {
     const Plan &p = *pl[s];
     ScanDev &S = host_scans[s];
@@ -134,17 +136,21 @@ int Solver::create(const std::vector<Plan *> &pl, const at_params &prm) {
     S.ctl = (Ctl *)cur;
     cur += align_up(sizeof(Ctl));
     fp_pref[s + 1] = fp_pref[s] + fp_ctas(S, rpt);
+    pix_pref[s + 1] = pix_pref[s] + pix_ctas(S);
     bp_pref[s + 1] = bp_pref[s] + bp_ctas(S);
     sino_pref[s + 1] = sino_pref[s] + (S.nbins + 255) / 256;
   }
   fp_total = fp_pref[nscans];
+  pix_total = pix_pref[nscans];
   bp_total = bp_pref[nscans];
   sino_total = sino_pref[nscans];
   AT_CUDA_TRY(cudaMalloc(&scans_d, sizeof(ScanDev) * nscans));
   AT_CUDA_TRY(cudaMemcpy(scans_d, host_scans.data(), sizeof(ScanDev) * nscans, cudaMemcpyHostToDevice));
-  AT_CUDA_TRY(cudaMalloc(&prefix_d, sizeof(int) * 3 * (nscans + 1)));
+  AT_CUDA_TRY(cudaMalloc(&prefix_d, sizeof(int) * 4 * (nscans + 1)));
   AT_CUDA_TRY(cudaMemcpy(prefix_d, fp_pref.data(), sizeof(int) * (nscans + 1), cudaMemcpyHostToDevice));
-  AT_CUDA_TRY(cudaMemcpy(prefix_d + (nscans + 1), bp_pref.data(), sizeof(int) * (nscans + 1), cudaMemcpyHostToDevice));
+  AT_CUDA_TRY(cudaMemcpy(prefix_d + (nscans + 1), pix_pref.data(), sizeof(int) * (nscans + 1), cudaMemcpyHostToDevice));
+  AT_CUDA_TRY(cudaMemcpy(prefix_d + 3 * (nscans + 1), bp_pref.data(), sizeof(int) * (nscans + 1),
+                         cudaMemcpyHostToDevice));
   AT_CUDA_TRY(cudaMemcpy(prefix_d + 2 * (nscans + 1), sino_pref.data(), sizeof(int) * (nscans + 1),
                          cudaMemcpyHostToDevice));
   return AT_OK;
@@ -174,7 +180,7 @@ int Solver::reset(cudaStream_t st) {
   if ((rc = reset_ctl(st))) return rc;
   Launch L = base_launch(1);
   L.flow = FLOW_ENABLED;
-  AT_CUDA_TRY(launch_pixel(PK_INIT, L, bp_total, st));
+  AT_CUDA_TRY(launch_pixel(PK_INIT, L, pix_total, st));
   return AT_OK;
 }
 
@@ -232,7 +238,7 @@ int Solver::enqueue_image(cudaStream_t st) {
     return AT_OK;
   };
   auto bp = [&](int stage, int u, int k) -> int {
-    Launch L = base_launch(1);
+    Launch L = base_launch(3);
     L.flow = FLOW_IMAGE;
     L.stage = stage;
     L.in_buf = B_R;
@@ -252,7 +258,7 @@ int Solver::enqueue_image(cudaStream_t st) {
     L.aux_buf = aux;
     L.k = k;
     L.flag = flag;
-    AT_CUDA_TRY(launch_pixel(which, L, which == PK_SINO ? sino_total : bp_total, st));
+    AT_CUDA_TRY(launch_pixel(which, L, which == PK_SINO ? sino_total : pix_total, st));
     launches++;
     return AT_OK;
   };
@@ -295,7 +301,7 @@ int Solver::enqueue_edge(cudaStream_t st) {
     L.flow = flow;
     L.stage = stage;
     L.k = k;
-    AT_CUDA_TRY(launch_pixel(which, L, bp_total, st));
+    AT_CUDA_TRY(launch_pixel(which, L, pix_total, st));
     launches++;
     return AT_OK;
   };

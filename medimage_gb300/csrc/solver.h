@@ -18,8 +18,8 @@ struct Solver {
   size_t arena_bytes = 0;
   std::vector<ScanDev> host_scans;
   ScanDev *scans_d = nullptr;
-  int *prefix_d = nullptr;  // [3][nscans+1]: forward-projector, pixel, sinogram CTA prefixes
-  int fp_total = 0, bp_total = 0, sino_total = 0;
+  int *prefix_d = nullptr;  // [4][nscans+1]: forward-projector, pixel-pass, sinogram-pass, back-projector CTAs
+  int fp_total = 0, pix_total = 0, sino_total = 0, bp_total = 0;
   cudaStream_t own_stream = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;

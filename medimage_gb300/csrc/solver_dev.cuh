@@ -82,8 +82,10 @@ struct ScanDev {
   const uint32_t *bits;
   const uint32_t *blk_word;
   const uint8_t *blk_nw;
-  const float4 *view;
-  float det_inv_pitch, det_t0, pixel_mm, pad1;
+  const uint4 *run;          // back-projection runs grouped by 16x16 tile
+  const int32_t *tile_off;
+  int ntiles_y;
+  float pixel_mm;
   // goldnc plan
   const GcSeg *gc_seg;
   const int32_t *gc_pair_off;

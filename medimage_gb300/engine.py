@@ -63,6 +63,8 @@ class _PlanStats(C.Structure):
         ("offgrid", C.c_int64),
         ("device_bytes", C.c_int64),
         ("max_segments", C.c_int32),
+        ("fp_rays_per_thread", C.c_int32),
+        ("bp_runs", C.c_int64),
     ]
 
 

@@ -156,6 +156,21 @@ int at_solver_launches_per_outer(const at_solver *s, int32_t *n);
 int at_reconstruct_host(const at_plan *plan, const at_params *params, const float *h_sino, float *h_f,
                         float *h_v);
 
+/* ---- forward projection that allocates no device memory ----
+ * No counterpart in the reference.  For callers that may not allocate device
+ * memory (their device memory belongs to another allocator's pool, or they
+ * run where cudaMalloc's implicit device synchronisation is not allowed):
+ * computes d_r = d_g - A d_img and *d_energy = sum (A d_img - d_g)^2 (FP64,
+ * device pointer) with the forward projector and its fused reduction, taking
+ * the reduction's scratch from a fixed 256 KiB array compiled into the
+ * library instead of allocating it.  Plans whose forward projection needs more
+ * than that (more than about 32,700 CTAs) are rejected with AT_EINVAL.  The
+ * first call on a device looks up the array's address (make it before any
+ * stream capture); calls share the array, so calls that overlap on the GPU
+ * race and must not be issued. */
+int at_forward_residual_noalloc(const at_plan *plan, const float *d_img, const float *d_g, float *d_r,
+                                double *d_energy, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

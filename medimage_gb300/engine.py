@@ -103,6 +103,8 @@ SIGNATURES = {
     "at_solver_trace": ([C.c_void_p, C.c_int32, _dp, C.c_int32, C.POINTER(C.c_int32)], C.c_int),
     "at_solver_launches_per_outer": ([C.c_void_p, C.POINTER(C.c_int32)], C.c_int),
     "at_reconstruct_host": ([C.c_void_p, C.POINTER(_Params), _fp, _fp, _fp], C.c_int),
+    "at_forward_residual_noalloc": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p],
+                                    C.c_int),
     # GoldenC drop-in (include/goldnc.h)
     "A": ([_dp, _dp], None),
     "AStar": ([_dp, _dp], None),

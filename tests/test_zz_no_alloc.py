@@ -1,0 +1,73 @@
+"""The forward-residual entry point that allocates nothing.
+
+Some callers cannot allocate device memory: their device memory is owned by
+another allocator's pool with a fixed budget, or they run in loops where
+cudaMalloc's implicit device synchronisation is not allowed.  For them
+at_forward_residual_noalloc takes its reduction scratch from a fixed array in
+the library.  Here it is called through the C-ABI twice in a row (different
+inputs each time, so the second call starts from the first call's leftovers in
+the shared array) and compared with the existing forward projector, at_forward:
+the residual must match it exactly (same kernel arithmetic), the FP64 energy
+to 1e-12 relative.  This file is collected last on purpose.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _dev(L, engine, arr):
+    p = C.c_void_p()
+    engine.engine._check("at_dev_alloc", L.at_dev_alloc(C.byref(p), arr.nbytes))
+    engine.engine._check("h2d", L.at_memcpy_h2d(p, arr.ctypes.data, arr.nbytes, None))
+    return p
+
+
+def _host(L, engine, dptr, shape, dtype):
+    out = np.zeros(shape, dtype)
+    engine.engine._check("d2h", L.at_memcpy_d2h(out.ctypes.data, dptr, out.nbytes, None))
+    engine.engine._check("sync", L.at_stream_sync(None))
+    return out
+
+
+@pytest.mark.parametrize("kind", ["fan", "goldnc"])
+def test_noalloc_forward_residual_matches_forward(engine, kind):
+    L = engine.lib()
+    if kind == "fan":
+        plan = engine.Plan.fan(engine.FanGeometry.covering(256, 1.0, 360, 512))
+    else:
+        plan = engine.Plan.goldnc()
+    n, nv, nd = plan.n, plan.nviews, plan.ndets
+    rng = np.random.default_rng(77)
+    bufs = []
+    for call in range(2):
+        img = engine.phantom.ellipse_phantom(n, seed=50 + call, n_random=5)
+        g = (rng.random((nv, nd)) * 4.0).astype(np.float32)
+        d_img, d_g = _dev(L, engine, img), _dev(L, engine, g)
+        d_r, d_e = _dev(L, engine, np.zeros((nv, nd), np.float32)), _dev(L, engine, np.zeros(1))
+        bufs += [d_img, d_g, d_r, d_e]
+        rc = L.at_forward_residual_noalloc(plan.handle, d_img, d_g, d_r, d_e, None)
+        assert rc == 0, L.at_last_error().decode()
+        r = _host(L, engine, d_r, (nv, nd), np.float32)
+        energy = float(_host(L, engine, d_e, (1,), np.float64)[0])
+        # the existing entry point
+        d_s = _dev(L, engine, np.zeros((nv, nd), np.float32))
+        bufs.append(d_s)
+        engine.engine._check("at_forward", L.at_forward(plan.handle, d_img, d_s, None))
+        a = _host(L, engine, d_s, (nv, nd), np.float32)
+        np.testing.assert_array_equal(r, g - a)
+        ref = float(np.sum((a.astype(np.float64) - g.astype(np.float64)) ** 2))
+        assert abs(energy - ref) <= 1e-12 * ref
+    for p in bufs:
+        L.at_dev_free(p)
+
+
+def test_noalloc_rejects_plans_beyond_its_scratch(engine):
+    L = engine.lib()
+    plan = engine.Plan.fan(engine.FanGeometry.covering(16, 1.0, 4096, 4096))
+    z = C.c_void_p(16)  # never dereferenced: the size check comes first
+    rc = L.at_forward_residual_noalloc(plan.handle, z, z, z, z, None)
+    assert rc == -1
+    assert "scratch" in L.at_last_error().decode()

@@ -26,6 +26,7 @@ namespace at {
 
 constexpr int kRayBlock = 128;  // rays per decision-bit block (one view)
 constexpr int kBpTile = 16;     // back-projection tile edge (pixels)
+constexpr int kBpViewBlock = 32;  // views whose contributions share one 32-bit accumulator
 
 // Per-ray header.  Boundary parameters are relative to the ray's entry
 // lambda_min (mm): the k-th x-plane crossing is at fmaf(k, lenx, ax), the k-th
@@ -63,11 +64,14 @@ struct Plan {
   uint8_t *blk_nw_d = nullptr;
   int nblocks_per_view = 0, nblocks = 0;
   // back projection: one entry per (ray, 16x16 tile) run of the traversal,
-  // grouped by tile, longest runs first.  Entry = {ray, k_in | nk << 16,
-  // cx_in | prev_step_was_x << 16, tile-local x | y << 4 | signx << 8 | signy << 9}
+  // grouped by tile, longest runs first.  Entry = {ray, k_in | nk << 14 |
+  // cx_in << 19, word offset of the ray's decision bits, tile-local x | y << 4
+  // | signx << 8 | signy << 9 | previous step was an x-step << 10}: the run
+  // starts at step k_in after cx_in x-crossings and covers nk segments
   uint4 *run_d = nullptr;
-  int32_t *tile_off_d = nullptr;  // [ntiles + 1]
-  int ntiles_y = 0, ntiles = 0;
+  int32_t *tile_off_d = nullptr;  // [ntiles * nvb + 1]: runs of (tile, view block)
+  int ntiles_y = 0, ntiles = 0, nvb = 0;
+  int bp_term_bits = 24;           // fixed-point bits of one back-projection term
   int64_t nruns = 0;
   // goldnc
   GcSeg *gc_seg_d = nullptr;

@@ -27,10 +27,10 @@ void fan_tables(const at_fan_geometry &g, double *scos, double *ssin, double *dc
 }
 
 int validate_fan(const at_fan_geometry &g) {
-  if (g.n < 8 || g.n > 16384) return set_error(AT_EINVAL, "fan geometry: n must be in [8, 16384]");
+  if (g.n < 8 || g.n > 8191) return set_error(AT_EINVAL, "fan geometry: n must be in [8, 8191]");
   if (g.nviews < 1 || g.nviews > 65536) return set_error(AT_EINVAL, "fan geometry: nviews must be in [1, 65536]");
-  if (g.ndets < 2 || g.ndets > 65536 || (g.ndets & 1))
-    return set_error(AT_EINVAL, "fan geometry: ndets must be even and in [2, 65536]");
+  if (g.ndets < 2 || g.ndets > 49152 || (g.ndets & 1))
+    return set_error(AT_EINVAL, "fan geometry: ndets must be even and in [2, 49152]");
   if (!(g.pixel_mm > 0) || !(g.sdd_mm > g.sod_mm) || !(g.det_pitch_deg > 0))
     return set_error(AT_EINVAL, "fan geometry: need pixel_mm > 0, sdd_mm > sod_mm, det_pitch_deg > 0");
   const double r = g.n * g.pixel_mm * std::sqrt(2.0) / 2.0;

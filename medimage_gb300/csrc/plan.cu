@@ -167,29 +167,34 @@ int dev_alloc(T **p, size_t count, int64_t &acct) {
 // ---------------------------------------------------------------------------
 template <int kMode>
 __global__ void fan_runs_kernel(int n, int nviews, int ndets, int nbpv, const RayHdr *hdr, const uint32_t *bits,
-                                const uint32_t *blk_word, int tiles_y, int *tile_count, unsigned long long *cursor,
-                                uint4 *ent, unsigned long long *keys) {
+                                const uint32_t *blk_word, int tiles_y, int nvb, int *tile_count,
+                                unsigned long long *cursor, uint4 *ent, unsigned long long *keys) {
   const int ray = blockIdx.x * blockDim.x + threadIdx.x;
   if (ray >= nviews * ndets) return;
   const RayHdr h = hdr[ray];
   if (h.nseg == 0) return;
   const int view = ray / ndets, det = ray % ndets;
-  const uint32_t *wp = bits + blk_word[view * nbpv + det / kRayBlock] + (det % kRayBlock);
+  const uint32_t wbase = blk_word[view * nbpv + det / kRayBlock] + (det % kRayBlock);
+  const uint32_t *wp = bits + wbase;
   int x = h.xy0 & 0xffff, y = h.xy0 >> 16;
   const int sx = (h.sgn & 1) ? 1 : -1, sy = (h.sgn & 2) ? 1 : -1;
-  int cx = 0, cur_tile = -1, run_k = 0, run_cx = 0, run_prevx = 0, run_lx = 0, run_ly = 0, last_bit = 0;
+  int cx = 0, cur_tile = -1, run_k = 0, run_cx = 0, run_x = 0, run_y = 0, prevx = 0, run_prevx = 0;
   uint32_t word = 0;
   auto close_run = [&](int k_end) {
     if (cur_tile < 0) return;
     const int nk = k_end - run_k;
+    const int vb = view / kBpViewBlock;
     if (kMode == 0) {
-      atomicAdd(&tile_count[cur_tile], 1);
+      atomicAdd(&tile_count[(size_t)cur_tile * nvb + vb], 1);
     } else {
       const unsigned long long pos = atomicAdd(cursor, 1ull);
-      ent[pos] = make_uint4((unsigned)ray, (unsigned)run_k | ((unsigned)nk << 16),
-                            (unsigned)run_cx | ((unsigned)run_prevx << 16),
-                            (unsigned)run_lx | ((unsigned)run_ly << 4) | ((h.sgn & 1u) << 8) | (((h.sgn >> 1) & 1u) << 9));
-      keys[pos] = ((unsigned long long)cur_tile << 38) | ((unsigned long long)(63 - nk) << 32) | (unsigned)ray;
+      ent[pos] = make_uint4((unsigned)ray, (unsigned)run_k | ((unsigned)nk << 14) | ((unsigned)run_cx << 19), wbase,
+                            (unsigned)(run_x & 15) | ((unsigned)(run_y & 15) << 4) | ((h.sgn & 1u) << 8) |
+                                (((h.sgn >> 1) & 1u) << 9) | ((unsigned)run_prevx << 10));
+      // by tile, then view block, then longest runs first, then ray order
+      keys[pos] = ((unsigned long long)cur_tile << 38) | ((unsigned long long)vb << 27) |
+                  ((unsigned long long)(63 - nk) << 21) | ((unsigned long long)(view % kBpViewBlock) << 16) |
+                  (unsigned)det;
     }
   };
   for (int k = 0; k < h.nseg; k++) {
@@ -201,9 +206,9 @@ __global__ void fan_runs_kernel(int n, int nviews, int ndets, int nbpv, const Ra
       cur_tile = t;
       run_k = k;
       run_cx = cx;
-      run_prevx = last_bit;
-      run_lx = x & 15;
-      run_ly = y & 15;
+      run_x = x;
+      run_y = y;
+      run_prevx = prevx;
     }
     const int bit = (word >> (k & 31)) & 1;
     if (bit) {
@@ -212,7 +217,7 @@ __global__ void fan_runs_kernel(int n, int nviews, int ndets, int nbpv, const Ra
     } else {
       y += sy;
     }
-    last_bit = bit;
+    prevx = bit;
   }
   close_run(h.nseg);
 }
@@ -231,27 +236,29 @@ int build_fan_runs(Plan &p, cudaStream_t st) {
   const int nrays = p.nviews * p.ndets, tpb = 128;
   p.ntiles_y = (p.n + kBpTile - 1) / kBpTile;
   p.ntiles = p.ntiles_y * p.ntiles_y;
+  p.nvb = (p.nviews + kBpViewBlock - 1) / kBpViewBlock;
+  const size_t ncell = (size_t)p.ntiles * p.nvb;
   int *cnt_d = nullptr;
   unsigned long long *cur_d = nullptr;
-  AT_CUDA_TRY(cudaMalloc(&cnt_d, sizeof(int) * p.ntiles));
+  AT_CUDA_TRY(cudaMalloc(&cnt_d, sizeof(int) * ncell));
   AT_CUDA_TRY(cudaMalloc(&cur_d, sizeof(unsigned long long)));
-  AT_CUDA_TRY(cudaMemsetAsync(cnt_d, 0, sizeof(int) * p.ntiles, st));
+  AT_CUDA_TRY(cudaMemsetAsync(cnt_d, 0, sizeof(int) * ncell, st));
   AT_CUDA_TRY(cudaMemsetAsync(cur_d, 0, sizeof(unsigned long long), st));
   fan_runs_kernel<0><<<(nrays + tpb - 1) / tpb, tpb, 0, st>>>(p.n, p.nviews, p.ndets, p.nblocks_per_view, p.rays_d,
-                                                              p.bits_d, p.blk_word_d, p.ntiles_y, cnt_d, nullptr,
-                                                              nullptr, nullptr);
+                                                              p.bits_d, p.blk_word_d, p.ntiles_y, p.nvb, cnt_d,
+                                                              nullptr, nullptr, nullptr);
   AT_CUDA_TRY(cudaGetLastError());
-  std::vector<int> cnt(p.ntiles);
-  AT_CUDA_TRY(cudaMemcpyAsync(cnt.data(), cnt_d, sizeof(int) * p.ntiles, cudaMemcpyDeviceToHost, st));
+  std::vector<int> cnt(ncell);
+  AT_CUDA_TRY(cudaMemcpyAsync(cnt.data(), cnt_d, sizeof(int) * ncell, cudaMemcpyDeviceToHost, st));
   AT_CUDA_TRY(cudaStreamSynchronize(st));
-  std::vector<int32_t> off(p.ntiles + 1);
+  std::vector<int32_t> off(ncell + 1);
   int64_t tot = 0;
-  for (int t = 0; t < p.ntiles; t++) {
+  for (size_t t = 0; t < ncell; t++) {
     off[t] = (int32_t)tot;
     tot += cnt[t];
   }
   if (tot >= (1ll << 31)) return set_error(AT_EINVAL, "plan: too many back-projection runs");
-  off[p.ntiles] = (int32_t)tot;
+  off[ncell] = (int32_t)tot;
   p.nruns = tot;
   uint4 *tmp_ent = nullptr;
   unsigned long long *keys = nullptr, *keys_out = nullptr;
@@ -262,12 +269,12 @@ int build_fan_runs(Plan &p, cudaStream_t st) {
   AT_CUDA_TRY(cudaMalloc(&idx, sizeof(unsigned) * std::max<int64_t>(tot, 1)));
   AT_CUDA_TRY(cudaMalloc(&idx_out, sizeof(unsigned) * std::max<int64_t>(tot, 1)));
   fan_runs_kernel<1><<<(nrays + tpb - 1) / tpb, tpb, 0, st>>>(p.n, p.nviews, p.ndets, p.nblocks_per_view, p.rays_d,
-                                                              p.bits_d, p.blk_word_d, p.ntiles_y, nullptr, cur_d,
-                                                              tmp_ent, keys);
+                                                              p.bits_d, p.blk_word_d, p.ntiles_y, p.nvb, nullptr,
+                                                              cur_d, tmp_ent, keys);
   AT_CUDA_TRY(cudaGetLastError());
   iota_kernel<<<(int)((tot + 255) / 256) + 1, 256, 0, st>>>(idx, tot);
   AT_CUDA_TRY(cudaGetLastError());
-  // keys are unique (tile, 63-nk, ray): the sorted order is deterministic
+  // keys are unique (tile, view block, 63-nk, view, det): the sorted order is deterministic
   size_t temp_bytes = 0;
   AT_CUDA_TRY(cub::DeviceRadixSort::SortPairs(nullptr, temp_bytes, keys, keys_out, idx, idx_out, (int64_t)tot, 0, 64, st));
   void *temp = nullptr;
@@ -275,10 +282,20 @@ int build_fan_runs(Plan &p, cudaStream_t st) {
   AT_CUDA_TRY(cub::DeviceRadixSort::SortPairs(temp, temp_bytes, keys, keys_out, idx, idx_out, (int64_t)tot, 0, 64, st));
   int rc;
   if ((rc = dev_alloc(&p.run_d, tot, p.device_bytes))) return rc;
-  if ((rc = dev_alloc(&p.tile_off_d, p.ntiles + 1, p.device_bytes))) return rc;
+  if ((rc = dev_alloc(&p.tile_off_d, ncell + 1, p.device_bytes))) return rc;
   gather_runs_kernel<<<(int)((tot + 255) / 256) + 1, 256, 0, st>>>(tmp_ent, idx_out, p.run_d, tot);
   AT_CUDA_TRY(cudaGetLastError());
-  AT_CUDA_TRY(cudaMemcpyAsync(p.tile_off_d, off.data(), sizeof(int32_t) * (p.ntiles + 1), cudaMemcpyHostToDevice, st));
+  AT_CUDA_TRY(cudaMemcpyAsync(p.tile_off_d, off.data(), sizeof(int32_t) * (ncell + 1), cudaMemcpyHostToDevice, st));
+  // Contributions one pixel can receive from one view: rays through a pixel are
+  // at least d_min * pitch apart (d_min = closest approach of the image to the
+  // source), so at most ceil(pixel diagonal / that) + 1 of them cross it.
+  const at_fan_geometry &g = p.geom;
+  const double dmin = g.sod_mm - g.n * g.pixel_mm * std::sqrt(2.0) / 2.0;
+  const double spacing = dmin * g.det_pitch_deg * M_PI / 180.0;
+  const int per_view = (int)std::ceil(std::sqrt(2.0) * g.pixel_mm / spacing) + 1;
+  const double per_block = (double)per_view * kBpViewBlock;
+  p.bp_term_bits = 31 - (int)std::ceil(std::log2(per_block + 1.0));
+  if (p.bp_term_bits < 16) return set_error(AT_EINVAL, "plan: detector far finer than the pixel grid (back projector precision)");
   AT_CUDA_TRY(cudaStreamSynchronize(st));
   cudaFree(temp);
   cudaFree(tmp_ent);
@@ -353,10 +370,12 @@ int build_fan_plan(Plan &p, cudaStream_t st) {
   p.offgrid = bad;
   p.max_segments = maxseg;
 
-  if ((rc = dev_alloc(&p.bits_d, words, p.device_bytes))) return rc;
+  // one spare block of zero words at the end: readers may fetch the word after
+  // a ray's last one without a bounds check
+  if ((rc = dev_alloc(&p.bits_d, words + kRayBlock, p.device_bytes))) return rc;
   if ((rc = dev_alloc(&p.blk_word_d, p.nblocks + 1, p.device_bytes))) return rc;
   if ((rc = dev_alloc(&p.blk_nw_d, p.nblocks, p.device_bytes))) return rc;
-  AT_CUDA_TRY(cudaMemsetAsync(p.bits_d, 0, sizeof(uint32_t) * std::max<uint64_t>(words, 1), st));
+  AT_CUDA_TRY(cudaMemsetAsync(p.bits_d, 0, sizeof(uint32_t) * (words + kRayBlock), st));
   AT_CUDA_TRY(cudaMemcpyAsync(p.blk_word_d, blk_word.data(), sizeof(uint32_t) * (p.nblocks + 1),
                               cudaMemcpyHostToDevice, st));
   AT_CUDA_TRY(cudaMemcpyAsync(p.blk_nw_d, blk_nw.data(), p.nblocks, cudaMemcpyHostToDevice, st));

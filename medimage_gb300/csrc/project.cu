@@ -220,13 +220,14 @@ __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
 // run of the traversal that crosses the tile, longest first; warps take 32
 // runs at a time and walk them with the forward walk's decision bits and
 // crossing formula, so each segment gets the forward projector's weight
-// bit-for-bit.  Each contribution w*r is scaled to a 31-bit integer (a power
-// of two chosen per tile from the largest |r| on its runs) and split into its
-// high part (>> 15) and low 15 bits, accumulated in two 32-bit shared-memory
-// integer accumulators; integer addition is associative, so the result does
-// not depend on the order in which lanes, warps or views arrive
-// (deterministic, no float atomics), and neither accumulator can overflow for
-// fewer than 32768 contributions per pixel.
+// bit-for-bit.  Runs are grouped in blocks of 32 views.  Each contribution w*r
+// is scaled to an integer (a power of two per tile, from the largest |r| on
+// its runs, sized so that one view block's contributions to a pixel cannot
+// overflow 32 bits) and added to a shared-memory 32-bit accumulator; after
+// each view block every thread folds its pixel into an exact 64-bit register
+// sum.  Integer addition is associative, so the result does not depend on the
+// order in which lanes, warps or views arrive (deterministic, no float
+// atomics).
 constexpr int kBpPitch = kBpTile + 1;  // padded row pitch of the accumulator
 
 __global__ void __launch_bounds__(256) fan_bp_kernel(const Launch L) {
@@ -237,81 +238,74 @@ __global__ void __launch_bounds__(256) fan_bp_kernel(const Launch L) {
   const int ncta = L.scans ? __ldg(L.prefix + scan + 1) - cta0 : gridDim.x;
   const int tile = blockIdx.x - cta0;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  __shared__ int acc_hi[kBpTile * kBpPitch], acc_lo[kBpTile * kBpPitch];
+  __shared__ int acc[kBpTile * kBpPitch];
   __shared__ float wmax[8];
-  for (int i = threadIdx.x; i < kBpTile * kBpPitch; i += blockDim.x) {
-    acc_hi[i] = 0;
-    acc_lo[i] = 0;
-  }
+  for (int i = threadIdx.x; i < kBpTile * kBpPitch; i += blockDim.x) acc[i] = 0;
   const float *__restrict__ sino = S.buf[L.in_buf];
-  const int e0 = __ldg(S.tile_off + tile), e1 = __ldg(S.tile_off + tile + 1);
+  const int32_t *toff = S.tile_off + (size_t)tile * S.nvb;
+  const int e0 = __ldg(toff), eN = __ldg(toff + S.nvb);
   // fixed-point scale from the largest |r| on the tile's runs
   float m = 0.f;
-  for (int i = e0 + threadIdx.x; i < e1; i += blockDim.x) m = fmaxf(m, fabsf(__ldg(sino + __ldg(&S.run[i].x))));
+  for (int i = e0 + threadIdx.x; i < eN; i += blockDim.x) m = fmaxf(m, fabsf(__ldg(sino + __ldg(&S.run[i].x))));
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
   if (lane == 0) wmax[warp] = m;
   __syncthreads();
   m = wmax[0];
   for (int w = 1; w < (int)(blockDim.x >> 5); w++) m = fmaxf(m, wmax[w]);
-  // every |w r| <= 1.5 * pixel * m < 2^ex; terms are scaled below 2^30
+  // every |w r| <= 1.5 * pixel * m < 2^ex; terms are scaled below 2^bp_term_bits,
+  // so one view block's terms fit a 32-bit accumulator without overflow
   int ex = 0;
   frexpf(fmaxf(1.5f * S.pixel_mm * m, 1e-30f), &ex);
-  const int sexp = min(30 - ex, 120);
+  const int sexp = min(S.bp_term_bits - ex, 120);
   const float scale = ldexpf(1.f, sexp);
+  const int own = (threadIdx.x >> 4) * kBpPitch + (threadIdx.x & 15);  // this thread's pixel
+  long long total = 0;  // exact sum over view blocks
   if (m > 0.f) {
-    for (int c = e0 + warp * 32; c < e1; c += blockDim.x) {
-      const int i = c + lane;
-      const bool valid = i < e1;
-      const uint4 e = valid ? __ldg(S.run + i) : make_uint4(0u, 0u, 0u, 0u);
-      const int nk = (int)(e.y >> 16);
-      const int ray = (int)e.x;
-      const int k_in = (int)(e.y & 0xffffu), cx_in = (int)(e.z & 0xffffu);
-      const int view = ray / S.ndets, det = ray - view * S.ndets;
-      const uint4 h1 = __ldg(reinterpret_cast<const uint4 *>(S.rays + ray) + 1);
-      const float ax = __uint_as_float(h1.x), ay = __uint_as_float(h1.y);
-      const float lx = __uint_as_float(h1.z), ly = __uint_as_float(h1.w);
-      const int blk = view * S.nbpv + (det >> 7);
-      const uint32_t *wp = S.bits + __ldg(S.blk_word + blk) + (det & (kRayBlock - 1));
-      const int wi = k_in >> 5;
-      uint32_t w0 = 0u, w1 = 0u;
-      if (valid) {
-        w0 = __ldg(wp + (size_t)wi * kRayBlock);
-        if (wi + 1 < (int)__ldg(S.blk_nw + blk)) w1 = __ldg(wp + (size_t)(wi + 1) * kRayBlock);
-      }
-      const uint32_t wnd = __funnelshift_r(w0, w1, k_in & 31);
-      const float rs = valid ? __ldg(sino + ray) * scale : 0.f;
-      float cxf = (float)cx_in, cyf = (float)(k_in - cx_in);
-      float prev = 0.f;
-      if (k_in > 0) prev = ((e.z >> 16) & 1u) ? fmaf(cxf - 1.f, lx, ax) : fmaf(cyf - 1.f, ly, ay);
-      int sidx = (int)(e.w & 15u) * kBpPitch + (int)((e.w >> 4) & 15u);
-      const int dsx = (e.w & 256u) ? kBpPitch : -kBpPitch, dsy = (e.w & 512u) ? 1 : -1;
-      const int steps = (int)__reduce_max_sync(0xffffffffu, (unsigned)nk);
-      for (int t = 0; t < steps; t++) {
-        const bool bx = (wnd >> t) & 1u;
-        const float nx = fmaf(cxf, lx, ax), ny = fmaf(cyf, ly, ay);
-        const float cur = bx ? nx : ny;
-        const float wt = cur - prev;
-        prev = cur;
-        if (t < nk) {
-          const int q = __float2int_rn(wt * rs);
-          atomicAdd(&acc_hi[sidx], q >> 15);
-          atomicAdd(&acc_lo[sidx], q & 0x7fff);
+    for (int vb = 0; vb < S.nvb; vb++) {
+      const int b0 = __ldg(toff + vb), b1 = __ldg(toff + vb + 1);
+      for (int c = b0 + warp * 32; c < b1; c += blockDim.x) {
+        const int i = c + lane;
+        const bool valid = i < b1;
+        const uint4 e = valid ? __ldg(S.run + i) : make_uint4(0u, 0u, 0u, 0u);
+        const int ray = (int)e.x;
+        const int k_in = (int)(e.y & 0x3fffu), nk = valid ? (int)((e.y >> 14) & 31u) : 0;
+        const int cx_in = (int)(e.y >> 19);
+        const uint4 h1 = __ldg(reinterpret_cast<const uint4 *>(S.rays + ray) + 1);
+        const float ax = __uint_as_float(h1.x), ay = __uint_as_float(h1.y);
+        const float lx = __uint_as_float(h1.z), ly = __uint_as_float(h1.w);
+        const uint32_t *wp = S.bits + e.z + (size_t)(k_in >> 5) * kRayBlock;
+        const uint32_t wnd = __funnelshift_r(__ldg(wp), __ldg(wp + kRayBlock), k_in & 31);
+        const float rs = __ldg(sino + ray) * scale;
+        float cxf = (float)cx_in, cyf = (float)(k_in - cx_in);
+        float prev = 0.f;
+        if (k_in > 0) prev = (e.w & 1024u) ? fmaf(cxf - 1.f, lx, ax) : fmaf(cyf - 1.f, ly, ay);
+        int sidx = (int)(e.w & 15u) * kBpPitch + (int)((e.w >> 4) & 15u);
+        const int dsx = (e.w & 256u) ? kBpPitch : -kBpPitch, dsy = (e.w & 512u) ? 1 : -1;
+        const int steps = (int)__reduce_max_sync(0xffffffffu, (unsigned)nk);
+        for (int t = 0; t < steps; t++) {
+          const bool bx = (wnd >> t) & 1u;
+          const float nx = fmaf(cxf, lx, ax), ny = fmaf(cyf, ly, ay);
+          const float cur = bx ? nx : ny;
+          const float wt = cur - prev;
+          prev = cur;
+          if (t < nk) atomicAdd(&acc[sidx], __float2int_rn(wt * rs));
+          sidx += bx ? dsx : dsy;
+          cxf += bx ? 1.f : 0.f;
+          cyf += bx ? 0.f : 1.f;
         }
-        sidx += bx ? dsx : dsy;
-        cxf += bx ? 1.f : 0.f;
-        cyf += bx ? 0.f : 1.f;
       }
+      __syncthreads();
+      total += acc[own];
+      acc[own] = 0;
+      __syncthreads();
     }
   }
-  __syncthreads();
   const int x = (tile / S.ntiles_y) * kBpTile + (threadIdx.x >> 4);
   const int y = (tile % S.ntiles_y) * kBpTile + (threadIdx.x & 15);
   double s0 = 0.0;
   if (x < S.n && y < S.n) {
-    const int j = (threadIdx.x >> 4) * kBpPitch + (threadIdx.x & 15);
-    const long long a = (long long)acc_hi[j] * 32768ll + (long long)acc_lo[j];
-    const float val = (float)((double)a * ldexp(1.0, -sexp));
+    const float val = (float)((double)total * ldexp(1.0, -sexp));
     bp_epilogue(S, L, x, y, val, s0);
   }
   if (stage_reduces(L.stage)) {

@@ -39,6 +39,8 @@ void fill_scan_plan(ScanDev &S, const Plan &p) {
   S.run = p.run_d;
   S.tile_off = p.tile_off_d;
   S.ntiles_y = p.ntiles_y;
+  S.nvb = p.nvb;
+  S.bp_term_bits = p.bp_term_bits;
   S.pixel_mm = (float)p.geom.pixel_mm;
   S.gc_seg = p.gc_seg_d;
   S.gc_pair_off = p.gc_pair_off_d;

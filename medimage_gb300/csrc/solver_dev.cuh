@@ -83,8 +83,8 @@ struct ScanDev {
   const uint32_t *blk_word;
   const uint8_t *blk_nw;
   const uint4 *run;          // back-projection runs grouped by 16x16 tile
-  const int32_t *tile_off;
-  int ntiles_y;
+  const int32_t *tile_off;   // [tile * nvb + view block]
+  int ntiles_y, nvb, bp_term_bits;
   float pixel_mm;
   // goldnc plan
   const GcSeg *gc_seg;

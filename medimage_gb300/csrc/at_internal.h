@@ -26,7 +26,7 @@ namespace at {
 
 constexpr int kRayBlock = 128;  // rays per decision-bit block (one view)
 constexpr int kBpTile = 16;     // back-projection tile edge (pixels)
-constexpr int kBpViewBlock = 32;  // views whose contributions share one 32-bit accumulator
+constexpr int kBpViewBlock = 64;  // views whose contributions share one 32-bit accumulator
 
 // Per-ray header.  Boundary parameters are relative to the ray's entry
 // lambda_min (mm): the k-th x-plane crossing is at fmaf(k, lenx, ax), the k-th

@@ -192,8 +192,9 @@ __global__ void fan_runs_kernel(int n, int nviews, int ndets, int nbpv, const Ra
                             (unsigned)(run_x & 15) | ((unsigned)(run_y & 15) << 4) | ((h.sgn & 1u) << 8) |
                                 (((h.sgn >> 1) & 1u) << 9) | ((unsigned)run_prevx << 10));
       // by tile, then view block, then longest runs first, then ray order
-      keys[pos] = ((unsigned long long)cur_tile << 38) | ((unsigned long long)vb << 27) |
-                  ((unsigned long long)(63 - nk) << 21) | ((unsigned long long)(view % kBpViewBlock) << 16) |
+      static_assert(kBpViewBlock <= 64, "view-in-block field is 6 bits");
+      keys[pos] = ((unsigned long long)cur_tile << 38) | ((unsigned long long)vb << 28) |
+                  ((unsigned long long)(63 - nk) << 22) | ((unsigned long long)(view % kBpViewBlock) << 16) |
                   (unsigned)det;
     }
   };

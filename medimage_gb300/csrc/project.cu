@@ -152,10 +152,12 @@ __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
       cx[r] = cy[r] = prev[r] = acc[r] = comp[r] = 0.f;
       my_max = max(my_max, nseg[r]);
     }
-    // warp-uniform trip count
-    unsigned mm = (unsigned)my_max;
-    mm = __reduce_max_sync(0xffffffffu, mm);
-    const int nwords = ((int)mm + 31) >> 5;
+    // warp-uniform trip count, and the words that are full for every ray
+    int my_min = nseg[0];
+#pragma unroll
+    for (int r = 1; r < RPT; r++) my_min = min(my_min, nseg[r]);
+    const int nwords = ((int)__reduce_max_sync(0xffffffffu, (unsigned)my_max) + 31) >> 5;
+    const int wfull = S.offgrid ? 0 : (int)(__reduce_min_sync(0xffffffffu, (unsigned)my_min) >> 5);
     const uint32_t *wp = S.bits + __ldg(S.blk_word + blk) + in_blk;
     for (int w = 0; w < nwords; w++) {
       uint32_t bw[RPT];
@@ -176,22 +178,43 @@ __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
 #pragma unroll
       for (int r = 0; r < RPT; r++) part[r] = 0.f;
       const int base = w << 5;
-#pragma unroll 8
-      for (int b = 0; b < 32; b++) {
+      if (w < wfull) {
+        // every ray of the warp has 32 segments in this word and (clean plan)
+        // no segment leaves the grid: no per-segment checks
 #pragma unroll
-        for (int r = 0; r < RPT; r++) {
-          const bool bx = (bw[r] >> b) & 1u;
-          const float nx = fmaf(cx[r], lx[r], ax[r]);
-          const float ny = fmaf(cy[r], ly[r], ay[r]);
-          const float cur = bx ? nx : ny;
-          const float wt = cur - prev[r];
-          prev[r] = cur;
-          const bool on = (base + b) < nseg[r] && (unsigned)idx[r] < npix;
-          const float val = on ? __ldg(img + idx[r]) : 0.f;
-          part[r] = fmaf(wt, val, part[r]);
-          idx[r] += bx ? stx[r] : sty[r];
-          cx[r] += bx ? 1.f : 0.f;
-          cy[r] += bx ? 0.f : 1.f;
+        for (int b = 0; b < 32; b++) {
+#pragma unroll
+          for (int r = 0; r < RPT; r++) {
+            const bool bx = (bw[r] >> b) & 1u;
+            const float nx = fmaf(cx[r], lx[r], ax[r]);
+            const float ny = fmaf(cy[r], ly[r], ay[r]);
+            const float cur = bx ? nx : ny;
+            const float wt = cur - prev[r];
+            prev[r] = cur;
+            part[r] = fmaf(wt, __ldg(img + idx[r]), part[r]);
+            idx[r] += bx ? stx[r] : sty[r];
+            cx[r] += bx ? 1.f : 0.f;
+            cy[r] += bx ? 0.f : 1.f;
+          }
+        }
+      } else {
+#pragma unroll 8
+        for (int b = 0; b < 32; b++) {
+#pragma unroll
+          for (int r = 0; r < RPT; r++) {
+            const bool bx = (bw[r] >> b) & 1u;
+            const float nx = fmaf(cx[r], lx[r], ax[r]);
+            const float ny = fmaf(cy[r], ly[r], ay[r]);
+            const float cur = bx ? nx : ny;
+            const float wt = cur - prev[r];
+            prev[r] = cur;
+            const bool on = (base + b) < nseg[r] && (unsigned)idx[r] < npix;
+            const float val = on ? __ldg(img + idx[r]) : 0.f;
+            part[r] = fmaf(wt, val, part[r]);
+            idx[r] += bx ? stx[r] : sty[r];
+            cx[r] += bx ? 1.f : 0.f;
+            cy[r] += bx ? 0.f : 1.f;
+          }
         }
       }
       // fold only words that hold segments of this ray, so the result does not
@@ -236,14 +259,16 @@ __global__ void __launch_bounds__(256) fan_bp_kernel(const Launch L) {
   if (!flow_active(S, L.flow)) return;
   const int cta0 = L.scans ? __ldg(L.prefix + scan) : 0;
   const int ncta = L.scans ? __ldg(L.prefix + scan + 1) - cta0 : gridDim.x;
-  const int tile = blockIdx.x - cta0;
+  const int local_cta = blockIdx.x - cta0;
+  const int tile = local_cta;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const bool real = tile < S.ntiles_y * S.ntiles_y;
   __shared__ int acc[kBpTile * kBpPitch];
   __shared__ float wmax[8];
   for (int i = threadIdx.x; i < kBpTile * kBpPitch; i += blockDim.x) acc[i] = 0;
   const float *__restrict__ sino = S.buf[L.in_buf];
-  const int32_t *toff = S.tile_off + (size_t)tile * S.nvb;
-  const int e0 = __ldg(toff), eN = __ldg(toff + S.nvb);
+  const int32_t *toff = S.tile_off + (size_t)(real ? tile : 0) * S.nvb;
+  const int e0 = real ? __ldg(toff) : 0, eN = real ? __ldg(toff + S.nvb) : 0;
   // fixed-point scale from the largest |r| on the tile's runs
   float m = 0.f;
   for (int i = e0 + threadIdx.x; i < eN; i += blockDim.x) m = fmaxf(m, fabsf(__ldg(sino + __ldg(&S.run[i].x))));
@@ -261,7 +286,7 @@ __global__ void __launch_bounds__(256) fan_bp_kernel(const Launch L) {
   const float scale = ldexpf(1.f, sexp);
   const int own = (threadIdx.x >> 4) * kBpPitch + (threadIdx.x & 15);  // this thread's pixel
   long long total = 0;  // exact sum over view blocks
-  if (m > 0.f) {
+  if (real && m > 0.f) {
     for (int vb = 0; vb < S.nvb; vb++) {
       const int b0 = __ldg(toff + vb), b1 = __ldg(toff + vb + 1);
       for (int c = b0 + warp * 32; c < b1; c += blockDim.x) {
@@ -283,6 +308,7 @@ __global__ void __launch_bounds__(256) fan_bp_kernel(const Launch L) {
         int sidx = (int)(e.w & 15u) * kBpPitch + (int)((e.w >> 4) & 15u);
         const int dsx = (e.w & 256u) ? kBpPitch : -kBpPitch, dsy = (e.w & 512u) ? 1 : -1;
         const int steps = (int)__reduce_max_sync(0xffffffffu, (unsigned)nk);
+#pragma unroll 4
         for (int t = 0; t < steps; t++) {
           const bool bx = (wnd >> t) & 1u;
           const float nx = fmaf(cxf, lx, ax), ny = fmaf(cyf, ly, ay);
@@ -304,13 +330,13 @@ __global__ void __launch_bounds__(256) fan_bp_kernel(const Launch L) {
   const int x = (tile / S.ntiles_y) * kBpTile + (threadIdx.x >> 4);
   const int y = (tile % S.ntiles_y) * kBpTile + (threadIdx.x & 15);
   double s0 = 0.0;
-  if (x < S.n && y < S.n) {
+  if (real && x < S.n && y < S.n) {
     const float val = (float)((double)total * ldexp(1.0, -sexp));
     bp_epilogue(S, L, x, y, val, s0);
   }
   if (stage_reduces(L.stage)) {
     double v[1] = {s0};
-    reduce_and_finalize<1>(S, L, v, tile, ncta);
+    reduce_and_finalize<1>(S, L, v, local_cta, ncta);
   }
 }
 

@@ -32,6 +32,7 @@ void fill_scan_plan(ScanDev &S, const Plan &p) {
   S.npix = p.n * p.n;
   S.nbins = p.nviews * p.ndets;
   S.nbpv = p.nblocks_per_view;
+  S.offgrid = p.offgrid ? 1 : 0;
   S.rays = p.rays_d;
   S.bits = p.bits_d;
   S.blk_word = p.blk_word_d;

@@ -76,7 +76,7 @@ constexpr int kTraceCap = 4096;  // records per scan (10 doubles each)
 
 struct ScanDev {
   int kind, n, nviews, ndets;
-  int npix, nbins, nbpv, pad0;
+  int npix, nbins, nbpv, offgrid;  // offgrid: the plan traces segments off the grid
   // fan plan
   const RayHdr *rays;
   const uint32_t *bits;

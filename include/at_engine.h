@@ -156,6 +156,41 @@ int at_solver_launches_per_outer(const at_solver *s, int32_t *n);
 int at_reconstruct_host(const at_plan *plan, const at_params *params, const float *h_sino, float *h_f,
                         float *h_v);
 
+/* ---- continuous-batching server ----
+ * Requests are admitted into a running batch once they have arrived and
+ * their device state fits the HBM budget and a slot is free; every round
+ * advances all admitted requests by one outer iteration with one launch per
+ * kernel for the whole mix; a finished request's f and v are copied out and
+ * its slot and memory go to the next request.  Each result is independent of
+ * the mix it ran in.  Reference counterpart: none (GoldenC runs one
+ * reconstruction per process, main.c:51-79); each request runs MumfordShah
+ * (main.c:35-49) on its own data. */
+typedef struct at_server at_server;
+typedef struct at_server_config {
+    size_t hbm_budget_bytes;  /* device state of admitted requests (plans not counted) */
+    int32_t max_active;       /* slots: requests advanced together                     */
+    double alpha, beta, epsilon;
+    int32_t iter_image, iter_edge, mode;
+    int32_t fp_rays_per_thread; /* forward-projector variant for the whole run (0 = 1)  */
+} at_server_config;
+typedef struct at_server_stats {
+    int64_t submitted, completed, rounds;
+    double p50_latency_s, p99_latency_s, max_latency_s; /* completion - arrival */
+    double slices_per_s;      /* completed / (last completion - first admitted arrival) */
+    double busy_s;            /* time spent in rounds                                   */
+    size_t peak_state_bytes;
+} at_server_stats;
+int at_server_create(const at_server_config *cfg, at_server **out);
+void at_server_destroy(at_server *s);
+/* Queues a request; arrival_s is relative to the server clock, which starts at
+ * the first at_server_run.  The sinogram is copied; the plan must outlive it. */
+int at_server_submit(at_server *s, at_plan *plan, const float *h_sino, int32_t iter_alt, double arrival_s,
+                     int64_t *id);
+/* Serves until every queued request is done (or max_seconds passed). */
+int at_server_run(at_server *s, double max_seconds);
+int at_server_result(at_server *s, int64_t id, float *h_f, float *h_v, double *latency_s, double *wait_s);
+int at_server_get_stats(const at_server *s, at_server_stats *out);
+
 /* ---- forward projection that allocates no device memory ----
  * No counterpart in the reference.  For callers that may not allocate device
  * memory (their device memory belongs to another allocator's pool, or they

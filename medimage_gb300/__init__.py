@@ -14,6 +14,7 @@ from .engine import (  # noqa: F401
     FanGeometry,
     Params,
     Plan,
+    Server,
     Solver,
     device_info,
     lib,
@@ -26,6 +27,7 @@ __all__ = [
     "FanGeometry",
     "Params",
     "Plan",
+    "Server",
     "Solver",
     "configs",
     "device_info",

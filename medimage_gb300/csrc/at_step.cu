@@ -307,3 +307,17 @@ cudaError_t launch_median(const float *in, float *out, int n, cudaStream_t st) {
 }
 
 }  // namespace at
+
+namespace at {
+
+__global__ void fill_kernel(float *p, float v, size_t n) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) p[i] = v;
+}
+
+cudaError_t launch_fill(float *p, float v, size_t n, cudaStream_t st) {
+  fill_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(p, v, n);
+  return cudaGetLastError();
+}
+
+}  // namespace at

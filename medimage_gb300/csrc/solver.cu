@@ -1,12 +1,13 @@
-// solver.cpp -- host orchestration of the batched AT solver.
+// solver.cu -- host orchestration of the batched AT solver.
 //
-// A solver owns, for each scan of its batch, the state buffers of
-// origin/GoldenC/src/main.c (f, v, d, p, update, r, q, ...) in one device
-// allocation, a control block with the CG scalars, and a trace buffer.  The
-// launch sequence of one outer iteration (image step then edge step,
-// main.c:43-47) is recorded once into a CUDA graph and replayed; early exits
-// are decided on the device, so later launches of a finished step return at
-// their first instruction.
+// Each scan of a batch owns the state buffers of origin/GoldenC/src/main.c
+// (f, v, d, p, update, r, q, ...), a control block with the CG scalars, FP64
+// partial sums and a trace buffer.  A Batch issues the launch sequence of one
+// outer iteration (image step then edge step, main.c:43-47) for a set of
+// scans; early exits are decided on the device, so later launches of a
+// finished step return at their first instruction.  A Solver keeps a fixed
+// batch in one allocation and captures its outer iteration once as a CUDA
+// graph; the server (server.cu) rebuilds its batch as requests come and go.
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -51,6 +52,7 @@ void fill_scan_plan(ScanDev &S, const Plan &p) {
 
 namespace {
 enum PixKernel { PK_UPD = 0, PK_PP, PK_COMMIT, PK_EDGE_INIT, PK_EDGE_D, PK_EDGE_UPD, PK_SINO, PK_INIT };
+enum Family { FAM_FP = 0, FAM_PIX = 1, FAM_SINO = 2, FAM_BP = 3 };
 
 size_t align_up(size_t x) { return (x + 255) & ~size_t(255); }
 
@@ -63,12 +65,8 @@ ScanLayout layout_of(const Plan &p, int rpt) {
   const size_t npix = (size_t)p.n * p.n, nbins = (size_t)p.nviews * p.ndets;
   L.img_bytes = align_up(npix * sizeof(float));
   L.sino_bytes = align_up(nbins * sizeof(float));
-  ScanDev tmp{};
-  tmp.kind = p.kind;
-  tmp.n = p.n;
-  tmp.nviews = p.nviews;
-  tmp.nbpv = p.nblocks_per_view;
-  tmp.ntiles_y = p.ntiles_y;
+  ScanDev tmp;
+  fill_scan_plan(tmp, p);
   const int maxcta = std::max({fp_ctas(tmp, rpt), bp_ctas(tmp), pix_ctas(tmp), (int)((nbins + 255) / 256)});
   L.partial_bytes = align_up((size_t)maxcta * 4 * sizeof(double));
   L.trace_bytes = align_up((size_t)kTraceCap * 10 * sizeof(double));
@@ -78,97 +76,78 @@ ScanLayout layout_of(const Plan &p, int rpt) {
 }
 }  // namespace
 
-int Solver::choose_rpt(const std::vector<Plan *> &plans) {
-  // rays per thread of the forward projector: the autotuned choice of the
-  // batch's first plan (projections are bitwise identical for every choice)
-  return plans.empty() ? 1 : plans[0]->fp_rpt;
+size_t scan_bytes(const Plan &p, int rpt) { return layout_of(p, rpt).total; }
+
+void carve_scan(ScanDev &S, const Plan &p, int rpt, char *cur) {
+  const ScanLayout lay = layout_of(p, rpt);
+  fill_scan_plan(S, p);
+  for (int b = 0; b < B_NIMG; b++) {
+    S.buf[b] = (float *)cur;
+    cur += lay.img_bytes;
+  }
+  for (int b = B_NIMG; b < B_NBUF; b++) {
+    S.buf[b] = (float *)cur;
+    cur += lay.sino_bytes;
+  }
+  S.partials = (double *)cur;
+  cur += lay.partial_bytes;
+  S.trace = (double *)cur;
+  cur += lay.trace_bytes;
+  S.ctl = (Ctl *)cur;
 }
 
-size_t Solver::footprint(const std::vector<Plan *> &plans, int rpt) {
-  size_t tot = 0;
-  for (auto *p : plans) tot += layout_of(*p, rpt).total;
-  return tot + 4096 * 4;
+Ctl make_ctl(const at_params &prm) {
+  Ctl c;
+  std::memset(&c, 0, sizeof(c));
+  c.enabled = 1;
+  c.iter_image = prm.iter_image;
+  c.iter_edge = prm.iter_edge;
+  c.median_every = prm.iter_image / 2;
+  c.mode = prm.mode;
+  c.alpha = prm.alpha;
+  c.beta = prm.beta;
+  c.eps = prm.epsilon;
+  return c;
 }
 
-int Solver::create(const std::vector<Plan *> &pl, const at_params &prm) {
-  if (pl.empty()) return set_error(AT_EINVAL, "solver: no scans");
-  const int kind = pl[0]->kind;
-  for (auto *p : pl)
-    if (p->kind != kind) return set_error(AT_EINVAL, "solver: a batch must hold one geometry kind");
-  if (prm.iter_image < 2) return set_error(AT_EINVAL, "solver: iter_image must be >= 2 (the reference divides by iter_image/2)");
-  if (prm.iter_edge < 1 || prm.iter_alt < 0) return set_error(AT_EINVAL, "solver: iteration counts must be positive");
-  if (prm.mode != 0 && prm.mode != 1) return set_error(AT_EINVAL, "solver: mode must be 0 (exact) or 1 (linear)");
-  plans = pl;
-  params = prm;
-  nscans = (int)pl.size();
-  rpt = choose_rpt(pl);
-  AT_CUDA_TRY(cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking));
+// ---------------------------------------------------------------- Batch
+Batch::~Batch() {
+  cudaFree(scans_d);
+  cudaFree(prefix_d);
+}
 
-  std::vector<ScanLayout> lay(nscans);
-  size_t total = 0;
-  for (int s = 0; s < nscans; s++) {
-    lay[s] = layout_of(*pl[s], rpt);
-    total += lay[s].total;
+int Batch::set(const ScanDev *scans, int n, int kind_, int rpt_, cudaStream_t st) {
+  if (n <= 0) return set_error(AT_EINVAL, "batch: no scans");
+  kind = kind_;
+  rpt = rpt_;
+  if (n > cap) {
+    cudaFree(scans_d);
+    cudaFree(prefix_d);
+    scans_d = nullptr;
+    prefix_d = nullptr;
+    cap = std::max(n, 2 * cap);
+    AT_CUDA_TRY(cudaMalloc(&scans_d, sizeof(ScanDev) * cap));
+    AT_CUDA_TRY(cudaMalloc(&prefix_d, sizeof(int) * 4 * (cap + 1)));
   }
-  if (cudaMalloc(&arena, total) != cudaSuccess) {
-    cudaGetLastError();
-    return set_error(AT_ENOMEM, "solver: device allocation of " + std::to_string(total) + " bytes failed");
+  nscans = n;
+  std::vector<int> pref(4 * (n + 1), 0);
+  for (int s = 0; s < n; s++) {
+    pref[FAM_FP * (n + 1) + s + 1] = pref[FAM_FP * (n + 1) + s] + fp_ctas(scans[s], rpt);
+    pref[FAM_PIX * (n + 1) + s + 1] = pref[FAM_PIX * (n + 1) + s] + pix_ctas(scans[s]);
+    pref[FAM_SINO * (n + 1) + s + 1] = pref[FAM_SINO * (n + 1) + s] + (scans[s].nbins + 255) / 256;
+    pref[FAM_BP * (n + 1) + s + 1] = pref[FAM_BP * (n + 1) + s] + bp_ctas(scans[s]);
   }
-  arena_bytes = total;
-  AT_CUDA_TRY(cudaMemset(arena, 0, total));
-  host_scans.resize(nscans);
-  char *cur = (char *)arena;
-  std::vector<int> fp_pref(nscans + 1, 0), pix_pref(nscans + 1, 0), sino_pref(nscans + 1, 0),
-      bp_pref(nscans + 1, 0);
-  for (int s = 0; s < nscans; s++) {
-    const Plan &p = *pl[s];
-    ScanDev &S = host_scans[s];
-    fill_scan_plan(S, p);
-    for (int b = 0; b < B_NIMG; b++) {
-      S.buf[b] = (float *)cur;
-      cur += lay[s].img_bytes;
-    }
-    for (int b = B_NIMG; b < B_NBUF; b++) {
-      S.buf[b] = (float *)cur;
-      cur += lay[s].sino_bytes;
-    }
-    S.partials = (double *)cur;
-    cur += lay[s].partial_bytes;
-    S.trace = (double *)cur;
-    cur += lay[s].trace_bytes;
-    S.ctl = (Ctl *)cur;
-    cur += align_up(sizeof(Ctl));
-    fp_pref[s + 1] = fp_pref[s] + fp_ctas(S, rpt);
-    pix_pref[s + 1] = pix_pref[s] + pix_ctas(S);
-    bp_pref[s + 1] = bp_pref[s] + bp_ctas(S);
-    sino_pref[s + 1] = sino_pref[s] + (S.nbins + 255) / 256;
-  }
-  fp_total = fp_pref[nscans];
-  pix_total = pix_pref[nscans];
-  bp_total = bp_pref[nscans];
-  sino_total = sino_pref[nscans];
-  AT_CUDA_TRY(cudaMalloc(&scans_d, sizeof(ScanDev) * nscans));
-  AT_CUDA_TRY(cudaMemcpy(scans_d, host_scans.data(), sizeof(ScanDev) * nscans, cudaMemcpyHostToDevice));
-  AT_CUDA_TRY(cudaMalloc(&prefix_d, sizeof(int) * 4 * (nscans + 1)));
-  AT_CUDA_TRY(cudaMemcpy(prefix_d, fp_pref.data(), sizeof(int) * (nscans + 1), cudaMemcpyHostToDevice));
-  AT_CUDA_TRY(cudaMemcpy(prefix_d + (nscans + 1), pix_pref.data(), sizeof(int) * (nscans + 1), cudaMemcpyHostToDevice));
-  AT_CUDA_TRY(cudaMemcpy(prefix_d + 3 * (nscans + 1), bp_pref.data(), sizeof(int) * (nscans + 1),
-                         cudaMemcpyHostToDevice));
-  AT_CUDA_TRY(cudaMemcpy(prefix_d + 2 * (nscans + 1), sino_pref.data(), sizeof(int) * (nscans + 1),
-                         cudaMemcpyHostToDevice));
+  fp_total = pref[FAM_FP * (n + 1) + n];
+  pix_total = pref[FAM_PIX * (n + 1) + n];
+  sino_total = pref[FAM_SINO * (n + 1) + n];
+  bp_total = pref[FAM_BP * (n + 1) + n];
+  // pageable sources: the copies are staged before cudaMemcpyAsync returns
+  AT_CUDA_TRY(cudaMemcpyAsync(scans_d, scans, sizeof(ScanDev) * n, cudaMemcpyHostToDevice, st));
+  AT_CUDA_TRY(cudaMemcpyAsync(prefix_d, pref.data(), sizeof(int) * pref.size(), cudaMemcpyHostToDevice, st));
   return AT_OK;
 }
 
-Solver::~Solver() {
-  if (graph_exec) cudaGraphExecDestroy(graph_exec);
-  if (graph) cudaGraphDestroy(graph);
-  cudaFree(arena);
-  cudaFree(scans_d);
-  cudaFree(prefix_d);
-  if (own_stream) cudaStreamDestroy(own_stream);
-}
-
-Launch Solver::base_launch(int family) const {
+Launch Batch::base_launch(int family) const {
   Launch L;
   std::memset(&L, 0, sizeof(L));
   L.scans = scans_d;
@@ -178,45 +157,15 @@ Launch Solver::base_launch(int family) const {
   return L;
 }
 
-int Solver::reset(cudaStream_t st) {
-  int rc;
-  if ((rc = reset_ctl(st))) return rc;
-  Launch L = base_launch(1);
+int Batch::enqueue_init(cudaStream_t st) {
+  Launch L = base_launch(FAM_PIX);
   L.flow = FLOW_ENABLED;
   AT_CUDA_TRY(launch_pixel(PK_INIT, L, pix_total, st));
   return AT_OK;
 }
 
-int Solver::reset_ctl(cudaStream_t st) {
-  std::vector<Ctl> ctl(nscans);
-  for (int s = 0; s < nscans; s++) {
-    Ctl &c = ctl[s];
-    std::memset(&c, 0, sizeof(c));
-    c.enabled = 1;
-    c.iter_image = params.iter_image;
-    c.iter_edge = params.iter_edge;
-    c.median_every = params.iter_image / 2;
-    c.mode = params.mode;
-    c.alpha = params.alpha;
-    c.beta = params.beta;
-    c.eps = params.epsilon;
-  }
-  // the control blocks are written from a host copy kept alive by the solver
-  ctl_host = ctl;
-  for (int s = 0; s < nscans; s++)
-    AT_CUDA_TRY(cudaMemcpyAsync(host_scans[s].ctl, &ctl_host[s], sizeof(Ctl), cudaMemcpyHostToDevice, st));
-  AT_CUDA_TRY(cudaStreamSynchronize(st));  // ctl_host may be rewritten by the next reset
-  return AT_OK;
-}
-
-int Solver::enable(int scan, bool on, cudaStream_t st) {
-  const int v = on ? 1 : 0;
-  AT_CUDA_TRY(cudaMemcpyAsync(&host_scans[scan].ctl->enabled, &v, sizeof(int), cudaMemcpyHostToDevice, st));
-  return AT_OK;
-}
-
 // The launch sequence of one outer iteration (main.c:45-46).
-int Solver::enqueue_outer(cudaStream_t st) {
+int Batch::enqueue_outer(cudaStream_t st) {
   launches = 0;
   int rc;
   if ((rc = enqueue_image(st))) return rc;
@@ -224,13 +173,12 @@ int Solver::enqueue_outer(cudaStream_t st) {
 }
 
 // minimize_in_IMAGE_variable, main.c:81-257
-int Solver::enqueue_image(cudaStream_t st) {
+int Batch::enqueue_image(cudaStream_t st) {
   const int K = params.iter_image;
   const bool linear = params.mode == 1;
-  const int kind = plans[0]->kind;
   const int m = K / 2;  // median every (int)(IterImage/2) iterations, main.c:180
   auto fp = [&](int stage, int in, int aux, int k) -> int {
-    Launch L = base_launch(0);
+    Launch L = base_launch(FAM_FP);
     L.flow = FLOW_IMAGE;
     L.stage = stage;
     L.in_buf = in;
@@ -241,7 +189,7 @@ int Solver::enqueue_image(cudaStream_t st) {
     return AT_OK;
   };
   auto bp = [&](int stage, int u, int k) -> int {
-    Launch L = base_launch(3);
+    Launch L = base_launch(FAM_BP);
     L.flow = FLOW_IMAGE;
     L.stage = stage;
     L.in_buf = B_R;
@@ -253,7 +201,7 @@ int Solver::enqueue_image(cudaStream_t st) {
     return AT_OK;
   };
   auto pix = [&](int which, int flow, int stage, int in, int out, int aux, int k, int flag) -> int {
-    Launch L = base_launch(which == PK_SINO ? 2 : 1);
+    Launch L = base_launch(which == PK_SINO ? FAM_SINO : FAM_PIX);
     L.flow = flow;
     L.stage = stage;
     L.in_buf = in;
@@ -297,10 +245,10 @@ int Solver::enqueue_image(cudaStream_t st) {
 }
 
 // minimize_in_EDGE_variable, main.c:259-360
-int Solver::enqueue_edge(cudaStream_t st) {
+int Batch::enqueue_edge(cudaStream_t st) {
   const int KE = params.iter_edge;
   auto pix = [&](int which, int flow, int stage, int k) -> int {
-    Launch L = base_launch(1);
+    Launch L = base_launch(FAM_PIX);
     L.flow = flow;
     L.stage = stage;
     L.k = k;
@@ -318,6 +266,90 @@ int Solver::enqueue_edge(cudaStream_t st) {
   }
   return AT_OK;
 }
+
+// ---------------------------------------------------------------- Solver
+int Solver::choose_rpt(const std::vector<Plan *> &plans) {
+  // rays per thread of the forward projector: the autotuned choice of the
+  // batch's first plan (projections are bitwise identical for every choice)
+  return plans.empty() ? 1 : plans[0]->fp_rpt;
+}
+
+size_t Solver::footprint(const std::vector<Plan *> &plans, int rpt) {
+  size_t tot = 0;
+  for (auto *p : plans) tot += scan_bytes(*p, rpt);
+  return tot + 4096 * 4;
+}
+
+int Solver::create(const std::vector<Plan *> &pl, const at_params &prm) {
+  if (pl.empty()) return set_error(AT_EINVAL, "solver: no scans");
+  const int kind = pl[0]->kind;
+  for (auto *p : pl)
+    if (p->kind != kind) return set_error(AT_EINVAL, "solver: a batch must hold one geometry kind");
+  if (prm.iter_image < 2) return set_error(AT_EINVAL, "solver: iter_image must be >= 2 (the reference divides by iter_image/2)");
+  if (prm.iter_edge < 1 || prm.iter_alt < 0) return set_error(AT_EINVAL, "solver: iteration counts must be positive");
+  if (prm.mode != 0 && prm.mode != 1) return set_error(AT_EINVAL, "solver: mode must be 0 (exact) or 1 (linear)");
+  plans = pl;
+  params = prm;
+  nscans = (int)pl.size();
+  rpt = choose_rpt(pl);
+  AT_CUDA_TRY(cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking));
+  size_t total = 0;
+  for (int s = 0; s < nscans; s++) total += scan_bytes(*pl[s], rpt);
+  if (cudaMalloc(&arena, total) != cudaSuccess) {
+    cudaGetLastError();
+    return set_error(AT_ENOMEM, "solver: device allocation of " + std::to_string(total) + " bytes failed");
+  }
+  arena_bytes = total;
+  AT_CUDA_TRY(cudaMemset(arena, 0, total));
+  host_scans.resize(nscans);
+  char *cur = (char *)arena;
+  for (int s = 0; s < nscans; s++) {
+    carve_scan(host_scans[s], *pl[s], rpt, cur);
+    cur += scan_bytes(*pl[s], rpt);
+  }
+  batch.params = prm;
+  int rc = batch.set(host_scans.data(), nscans, kind, rpt, own_stream);
+  if (rc) return rc;
+  AT_CUDA_TRY(cudaStreamSynchronize(own_stream));
+  return AT_OK;
+}
+
+Solver::~Solver() {
+  if (graph_exec) cudaGraphExecDestroy(graph_exec);
+  if (graph) cudaGraphDestroy(graph);
+  cudaFree(arena);
+  if (own_stream) cudaStreamDestroy(own_stream);
+}
+
+int Solver::reset(cudaStream_t st) {
+  int rc;
+  if ((rc = reset_ctl(st))) return rc;
+  return batch.enqueue_init(st);
+}
+
+int Solver::reset_ctl(cudaStream_t st) {
+  ctl_host.assign(nscans, make_ctl(params));
+  for (int s = 0; s < nscans; s++)
+    AT_CUDA_TRY(cudaMemcpyAsync(host_scans[s].ctl, &ctl_host[s], sizeof(Ctl), cudaMemcpyHostToDevice, st));
+  AT_CUDA_TRY(cudaStreamSynchronize(st));  // ctl_host may be rewritten by the next reset
+  return AT_OK;
+}
+
+int Solver::enable(int scan, bool on, cudaStream_t st) {
+  const int v = on ? 1 : 0;
+  AT_CUDA_TRY(cudaMemcpyAsync(&host_scans[scan].ctl->enabled, &v, sizeof(int), cudaMemcpyHostToDevice, st));
+  AT_CUDA_TRY(cudaStreamSynchronize(st));
+  return AT_OK;
+}
+
+int Solver::enqueue_outer(cudaStream_t st) {
+  const int rc = batch.enqueue_outer(st);
+  launches = batch.launches;
+  return rc;
+}
+
+int Solver::enqueue_image(cudaStream_t st) { return batch.enqueue_image(st); }
+int Solver::enqueue_edge(cudaStream_t st) { return batch.enqueue_edge(st); }
 
 int Solver::ensure_graph(cudaStream_t st) {
   if (graph_exec) return AT_OK;

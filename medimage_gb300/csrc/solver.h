@@ -1,4 +1,5 @@
-// solver.h -- host-side batched AT solver (see solver.cu).
+// solver.h -- host side of the batched AT solver (solver.cu) and of the
+// continuous-batching server (server.cu).
 #pragma once
 
 #include <vector>
@@ -8,18 +9,46 @@
 namespace at {
 
 void fill_scan_plan(ScanDev &S, const Plan &p);
+// device bytes of one scan's state (images, sinograms, partials, trace, control)
+size_t scan_bytes(const Plan &p, int rpt);
+// points S's state buffers into `mem` (scan_bytes(p, rpt) bytes, 256-aligned)
+void carve_scan(ScanDev &S, const Plan &p, int rpt, char *mem);
+// control block of a fresh reconstruction
+Ctl make_ctl(const at_params &prm);
 
+// The launch sequence of the AT iteration over a set of scans: one launch per
+// kernel for the whole set, per-scan CTA ranges from prefix tables.
+struct Batch {
+  at_params params{};
+  int kind = AT_GEOM_FAN, rpt = 1, nscans = 0, cap = 0;
+  ScanDev *scans_d = nullptr;
+  int *prefix_d = nullptr;  // [4][cap+1]: forward-projector, pixel-pass, sinogram-pass, back-projector CTAs
+  int fp_total = 0, pix_total = 0, sino_total = 0, bp_total = 0;
+  int launches = 0;         // kernel launches of the last enqueue_outer
+  Batch() = default;
+  Batch(const Batch &) = delete;
+  Batch &operator=(const Batch &) = delete;
+  ~Batch();
+  int set(const ScanDev *scans, int n, int kind, int rpt, cudaStream_t st);
+  Launch base_launch(int family) const;
+  int enqueue_init(cudaStream_t st);
+  int enqueue_outer(cudaStream_t st);
+  int enqueue_image(cudaStream_t st);
+  int enqueue_edge(cudaStream_t st);
+};
+
+// A fixed batch of scans in one device allocation, its outer iteration
+// captured once as a CUDA graph.
 struct Solver {
   std::vector<Plan *> plans;
   at_params params{};
   int nscans = 0;
-  int rpt = 1;  // rays per thread of the forward projector
+  int rpt = 1;
   void *arena = nullptr;
   size_t arena_bytes = 0;
   std::vector<ScanDev> host_scans;
-  ScanDev *scans_d = nullptr;
-  int *prefix_d = nullptr;  // [4][nscans+1]: forward-projector, pixel-pass, sinogram-pass, back-projector CTAs
-  int fp_total = 0, pix_total = 0, sino_total = 0, bp_total = 0;
+  std::vector<Ctl> ctl_host;  // staging for control-block uploads
+  Batch batch;
   cudaStream_t own_stream = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
@@ -29,8 +58,6 @@ struct Solver {
   static size_t footprint(const std::vector<Plan *> &plans, int rpt);
   int create(const std::vector<Plan *> &plans, const at_params &prm);
   ~Solver();
-  Launch base_launch(int family) const;
-  std::vector<Ctl> ctl_host;  // staging for control-block uploads
   int reset(cudaStream_t st);
   int reset_ctl(cudaStream_t st);
   int enable(int scan, bool on, cudaStream_t st);

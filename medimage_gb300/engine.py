@@ -68,6 +68,34 @@ class _PlanStats(C.Structure):
     ]
 
 
+class _ServerConfig(C.Structure):
+    _fields_ = [
+        ("hbm_budget_bytes", C.c_size_t),
+        ("max_active", C.c_int32),
+        ("alpha", C.c_double),
+        ("beta", C.c_double),
+        ("epsilon", C.c_double),
+        ("iter_image", C.c_int32),
+        ("iter_edge", C.c_int32),
+        ("mode", C.c_int32),
+        ("fp_rays_per_thread", C.c_int32),
+    ]
+
+
+class _ServerStats(C.Structure):
+    _fields_ = [
+        ("submitted", C.c_int64),
+        ("completed", C.c_int64),
+        ("rounds", C.c_int64),
+        ("p50_latency_s", C.c_double),
+        ("p99_latency_s", C.c_double),
+        ("max_latency_s", C.c_double),
+        ("slices_per_s", C.c_double),
+        ("busy_s", C.c_double),
+        ("peak_state_bytes", C.c_size_t),
+    ]
+
+
 # exported symbol -> (argtypes, restype); the table doubles as the ABI list the
 # CPU tests compare with include/*.h
 SIGNATURES = {
@@ -105,6 +133,12 @@ SIGNATURES = {
     "at_reconstruct_host": ([C.c_void_p, C.POINTER(_Params), _fp, _fp, _fp], C.c_int),
     "at_forward_residual_noalloc": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p],
                                     C.c_int),
+    "at_server_create": ([C.POINTER(_ServerConfig), C.POINTER(C.c_void_p)], C.c_int),
+    "at_server_destroy": ([C.c_void_p], None),
+    "at_server_submit": ([C.c_void_p, C.c_void_p, _fp, C.c_int32, C.c_double, C.POINTER(C.c_int64)], C.c_int),
+    "at_server_run": ([C.c_void_p, C.c_double], C.c_int),
+    "at_server_result": ([C.c_void_p, C.c_int64, _fp, _fp, C.POINTER(C.c_double), C.POINTER(C.c_double)], C.c_int),
+    "at_server_get_stats": ([C.c_void_p, C.POINTER(_ServerStats)], C.c_int),
     # GoldenC drop-in (include/goldnc.h)
     "A": ([_dp, _dp], None),
     "AStar": ([_dp, _dp], None),
@@ -368,3 +402,51 @@ def reconstruct(plan: Plan, params: Params, sino: np.ndarray):
     prm = params.c()
     _check("at_reconstruct_host", lib().at_reconstruct_host(plan.handle, C.byref(prm), sino, f, v))
     return f, v
+
+
+class Server:
+    """Continuous-batching reconstruction server (at_server_*)."""
+
+    def __init__(self, hbm_budget_bytes: int, max_active: int, params: Params | None = None,
+                 fp_rays_per_thread: int = 1):
+        p = params or Params()
+        cfg = _ServerConfig(hbm_budget_bytes, max_active, p.alpha, p.beta, p.epsilon, p.iter_image, p.iter_edge,
+                            p.mode, fp_rays_per_thread)
+        self._h = C.c_void_p()
+        _check("at_server_create", lib().at_server_create(C.byref(cfg), C.byref(self._h)))
+        self._plans = {}
+
+    def close(self):
+        if self._h:
+            lib().at_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, plan: Plan, sino: np.ndarray, iter_alt: int, arrival_s: float = 0.0) -> int:
+        sino = np.ascontiguousarray(sino, np.float32)
+        rid = C.c_int64()
+        _check("at_server_submit", lib().at_server_submit(self._h, plan.handle, sino, iter_alt, arrival_s,
+                                                          C.byref(rid)))
+        self._plans[rid.value] = plan
+        return rid.value
+
+    def run(self, max_seconds: float = 0.0) -> None:
+        _check("at_server_run", lib().at_server_run(self._h, max_seconds))
+
+    def result(self, rid: int):
+        p = self._plans[rid]
+        f = np.zeros((p.n, p.n), np.float32)
+        v = np.zeros((p.n, p.n), np.float32)
+        lat, wait = C.c_double(), C.c_double()
+        _check("at_server_result", lib().at_server_result(self._h, rid, f, v, C.byref(lat), C.byref(wait)))
+        return f, v, lat.value, wait.value
+
+    def stats(self) -> dict:
+        st = _ServerStats()
+        _check("at_server_get_stats", lib().at_server_get_stats(self._h, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in _ServerStats._fields_}

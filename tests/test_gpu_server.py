@@ -1,0 +1,63 @@
+"""The continuous-batching server: requests arriving while others run join the
+batch as slots and budget free up; every result must equal the same request
+served alone (bitwise: a request's arithmetic does not depend on the mix) and
+the fixed-batch solver's result within 1e-6."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def make_requests(engine, oracle):
+    G = engine.FanGeometry.covering
+    geoms = [G(64, 3.0, 90, 128), G(96, 2.0, 120, 160), G(80, 2.4, 72, 100)]
+    plans = [engine.Plan.fan(g) for g in geoms]
+    reqs = []
+    for i in range(7):
+        g, p = geoms[i % 3], plans[i % 3]
+        ph = engine.phantom.ellipse_phantom(g.n, seed=300 + i, n_random=3)
+        clean = oracle.fan_A(oracle.fan_from_engine(g), ph.astype(np.float64))
+        sino = engine.phantom.poisson_sinogram(clean, 1e4, 400 + i)
+        reqs.append((p, sino, 2 + (i % 3), 0.002 * i))
+    return plans, reqs
+
+
+def test_server_mix_equals_alone(engine, oracle):
+    plans, reqs = make_requests(engine, oracle)
+    srv = engine.Server(hbm_budget_bytes=1 << 34, max_active=3)
+    ids = [srv.submit(p, s, it, arr) for (p, s, it, arr) in reqs]
+    srv.run()
+    st = srv.stats()
+    assert st["completed"] == len(reqs)
+    assert st["p99_latency_s"] >= st["p50_latency_s"] > 0
+    for rid, (p, s, it, _) in zip(ids, reqs):
+        f_mix, v_mix, lat, wait = srv.result(rid)
+        assert lat > 0 and wait >= 0
+        alone = engine.Server(hbm_budget_bytes=1 << 34, max_active=1)
+        a = alone.submit(p, s, it, 0.0)
+        alone.run()
+        f_one, v_one, _, _ = alone.result(a)
+        np.testing.assert_array_equal(f_mix, f_one)
+        np.testing.assert_array_equal(v_mix, v_one)
+        solver = engine.Solver([p], engine.Params(iter_alt=it))
+        solver.set_sino(0, s)
+        solver.run()
+        f_s, v_s = solver.get(0)
+        assert np.linalg.norm(f_mix - f_s) <= 1e-6 * np.linalg.norm(f_s)
+        assert np.linalg.norm(v_mix - v_s) <= 1e-6 * np.linalg.norm(v_s)
+
+
+def test_server_admission_respects_budget(engine, oracle):
+    plans, reqs = make_requests(engine, oracle)
+    one = engine.Solver.footprint([plans[1]])  # largest of the three geometries
+    srv = engine.Server(hbm_budget_bytes=int(2.2 * one), max_active=8)
+    for (p, s, it, arr) in reqs:
+        srv.submit(p, s, it, 0.0)
+    srv.run()
+    st = srv.stats()
+    assert st["completed"] == len(reqs)
+    assert st["peak_state_bytes"] <= int(2.2 * one)
+    tiny = engine.Server(hbm_budget_bytes=1024, max_active=2)
+    with pytest.raises(engine.AtError) as ei:
+        tiny.submit(plans[0], reqs[0][1], 2, 0.0)
+    assert ei.value.code == -5

@@ -295,7 +295,8 @@ int build_fan_runs(Plan &p, cudaStream_t st) {
   const double spacing = dmin * g.det_pitch_deg * M_PI / 180.0;
   const int per_view = (int)std::ceil(std::sqrt(2.0) * g.pixel_mm / spacing) + 1;
   const double per_block = (double)per_view * kBpViewBlock;
-  p.bp_term_bits = 31 - (int)std::ceil(std::log2(per_block + 1.0));
+  // terms stay below 2^22 so the kernel can round them with one FFMA
+  p.bp_term_bits = std::min(22, 31 - (int)std::ceil(std::log2(per_block + 1.0)));
   if (p.bp_term_bits < 16) return set_error(AT_EINVAL, "plan: detector far finer than the pixel grid (back projector precision)");
   AT_CUDA_TRY(cudaStreamSynchronize(st));
   cudaFree(temp);

@@ -252,6 +252,10 @@ __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
 // order in which lanes, warps or views arrive (deterministic, no float
 // atomics).
 constexpr int kBpPitch = kBpTile + 1;  // padded row pitch of the accumulator
+// accumulator copies, chosen by lane: adjacent lanes (adjacent rays of one
+// view, often in the same pixel at the same step) never share an address
+constexpr int kBpCopies = 2;
+constexpr int kBpAccWords = kBpTile * kBpPitch;
 
 __global__ void __launch_bounds__(256) fan_bp_kernel(const Launch L) {
   const int scan = L.scans ? find_scan(L.prefix, L.nscans, blockIdx.x) : 0;
@@ -263,9 +267,10 @@ __global__ void __launch_bounds__(256) fan_bp_kernel(const Launch L) {
   const int tile = local_cta;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const bool real = tile < S.ntiles_y * S.ntiles_y;
-  __shared__ int acc[kBpTile * kBpPitch];
+  __shared__ int acc[kBpCopies * kBpAccWords];
   __shared__ float wmax[8];
-  for (int i = threadIdx.x; i < kBpTile * kBpPitch; i += blockDim.x) acc[i] = 0;
+  for (int i = threadIdx.x; i < kBpCopies * kBpAccWords; i += blockDim.x) acc[i] = 0;
+  int *const my_acc = acc + (lane % kBpCopies) * kBpAccWords;
   const float *__restrict__ sino = S.buf[L.in_buf];
   const int32_t *toff = S.tile_off + (size_t)(real ? tile : 0) * S.nvb;
   const int e0 = real ? __ldg(toff) : 0, eN = real ? __ldg(toff + S.nvb) : 0;
@@ -286,22 +291,37 @@ __global__ void __launch_bounds__(256) fan_bp_kernel(const Launch L) {
   const float scale = ldexpf(1.f, sexp);
   const int own = (threadIdx.x >> 4) * kBpPitch + (threadIdx.x & 15);  // this thread's pixel
   long long total = 0;  // exact sum over view blocks
+  // w*r*scale + 1.5*2^23 rounds w*r*scale to an integer in the float's low
+  // mantissa bits (|w*r*scale| < 2^22), so one FFMA does the scaling and the
+  // round-to-nearest conversion
+  constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
+  constexpr int kMagicBits = 0x4B400000;
   if (real && m > 0.f) {
     for (int vb = 0; vb < S.nvb; vb++) {
       const int b0 = __ldg(toff + vb), b1 = __ldg(toff + vb + 1);
-      for (int c = b0 + warp * 32; c < b1; c += blockDim.x) {
-        const int i = c + lane;
-        const bool valid = i < b1;
-        const uint4 e = valid ? __ldg(S.run + i) : make_uint4(0u, 0u, 0u, 0u);
-        const int ray = (int)e.x;
+      // two-stage pipeline: the next chunk's dependent loads fly during this walk
+      const uint4 kZ = make_uint4(0u, 0u, 0u, 0u);
+      int c = b0 + warp * 32;
+      uint4 e = (c + lane < b1) ? __ldg(S.run + c + lane) : kZ;
+      uint4 h1 = __ldg(reinterpret_cast<const uint4 *>(S.rays + e.x) + 1);
+      const uint32_t *wq = S.bits + e.z + (size_t)((e.y & 0x3fffu) >> 5) * kRayBlock;
+      uint32_t w0 = __ldg(wq), w1 = __ldg(wq + kRayBlock);
+      float r0 = __ldg(sino + e.x);
+      for (; c < b1; c += blockDim.x) {
+        const int cn = c + blockDim.x;
+        const uint4 en = (cn + lane < b1) ? __ldg(S.run + cn + lane) : kZ;
+        const uint4 h1n = __ldg(reinterpret_cast<const uint4 *>(S.rays + en.x) + 1);
+        const uint32_t *wn = S.bits + en.z + (size_t)((en.y & 0x3fffu) >> 5) * kRayBlock;
+        const uint32_t w0n = __ldg(wn), w1n = __ldg(wn + kRayBlock);
+        const float rn = __ldg(sino + en.x);
+        const bool valid = c + lane < b1;
+        const float rv = r0;
         const int k_in = (int)(e.y & 0x3fffu), nk = valid ? (int)((e.y >> 14) & 31u) : 0;
         const int cx_in = (int)(e.y >> 19);
-        const uint4 h1 = __ldg(reinterpret_cast<const uint4 *>(S.rays + ray) + 1);
         const float ax = __uint_as_float(h1.x), ay = __uint_as_float(h1.y);
         const float lx = __uint_as_float(h1.z), ly = __uint_as_float(h1.w);
-        const uint32_t *wp = S.bits + e.z + (size_t)(k_in >> 5) * kRayBlock;
-        const uint32_t wnd = __funnelshift_r(__ldg(wp), __ldg(wp + kRayBlock), k_in & 31);
-        const float rs = __ldg(sino + ray) * scale;
+        uint32_t wnd = __funnelshift_r(w0, w1, k_in & 31);
+        const float rs = rv * scale;
         float cxf = (float)cx_in, cyf = (float)(k_in - cx_in);
         float prev = 0.f;
         if (k_in > 0) prev = (e.w & 1024u) ? fmaf(cxf - 1.f, lx, ax) : fmaf(cyf - 1.f, ly, ay);
@@ -310,20 +330,29 @@ __global__ void __launch_bounds__(256) fan_bp_kernel(const Launch L) {
         const int steps = (int)__reduce_max_sync(0xffffffffu, (unsigned)nk);
 #pragma unroll 4
         for (int t = 0; t < steps; t++) {
-          const bool bx = (wnd >> t) & 1u;
+          const bool bx = wnd & 1u;
+          wnd >>= 1;
           const float nx = fmaf(cxf, lx, ax), ny = fmaf(cyf, ly, ay);
           const float cur = bx ? nx : ny;
           const float wt = cur - prev;
           prev = cur;
-          if (t < nk) atomicAdd(&acc[sidx], __float2int_rn(wt * rs));
+          if (t < nk) atomicAdd(&my_acc[sidx], __float_as_int(fmaf(wt, rs, kMagic)) - kMagicBits);
           sidx += bx ? dsx : dsy;
           cxf += bx ? 1.f : 0.f;
           cyf += bx ? 0.f : 1.f;
         }
+        e = en;
+        h1 = h1n;
+        w0 = w0n;
+        w1 = w1n;
+        r0 = rn;
       }
       __syncthreads();
-      total += acc[own];
-      acc[own] = 0;
+#pragma unroll
+      for (int cpy = 0; cpy < kBpCopies; cpy++) {
+        total += acc[cpy * kBpAccWords + own];
+        acc[cpy * kBpAccWords + own] = 0;
+      }
       __syncthreads();
     }
   }

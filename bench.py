@@ -101,6 +101,24 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def reduce_max(x: float, device="cpu") -> float:
+    """Max over ranks (the slowest replica sets the whole-job time)."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank: float, seconds: float, world: int) -> float:
+    """Replicas only: every rank processes its own units; the job's rate is all
+    units over the slowest rank's time."""
+    return units_per_rank * world / seconds
+
+
 def measured_peak_hbm():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
@@ -183,13 +201,9 @@ def run_ours(args):
         torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
-    ms = ev0.elapsed_time(ev1)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = reduce_max(ev0.elapsed_time(ev1), device="cuda")
     slices = args.steps * B * world
-    value = slices / (ms / 1e3)
+    value = whole_job_rate(args.steps * B, ms / 1e3, world)
     f0, v0 = solver.get(0, stream=st)
     psnr = mg.phantom.psnr(f0, phantoms[0])
     tr = solver.trace(0)
@@ -220,12 +234,8 @@ def run_ours(args):
     for _ in range(args.steps):
         e2e_step()
     torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = slices / e2e_s
+    e2e_s = reduce_max(time.perf_counter() - t0, device="cuda")
+    e2e_value = whole_job_rate(args.steps * B, e2e_s, world)
     del fp32
 
     # ---- roofline: the dominant kernel alone, same workload, CUDA events

@@ -1,0 +1,31 @@
+"""The GoldenC drop-in as a program uses it: a GoldenC-style C driver
+(tests/goldnc_driver.c: globals f, v, gDelta; g = A(phantom); MumfordShah)
+compiled against libat_engine.so and run, compared with the FP64 oracle of
+GoldenC's solver and projector (rel-L2 <= 1e-4)."""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.mark.skipif(shutil.which("gcc") is None, reason="no C compiler")
+def test_goldnc_program_through_the_library(engine, oracle, tmp_path):
+    lib_dir = os.path.join(ROOT, "medimage_gb300")
+    exe = tmp_path / "driver"
+    subprocess.run(["gcc", "-O2", "-std=c99", f"-I{ROOT}/include", os.path.join(ROOT, "tests", "goldnc_driver.c"),
+                    f"-L{lib_dir}", "-lat_engine", f"-Wl,-rpath,{lib_dir}", "-lm", "-o", str(exe)], check=True)
+    ph = engine.phantom.ellipse_phantom(512, seed=61).astype(np.float64)
+    (tmp_path / "ph.bin").write_bytes(ph.tobytes())
+    subprocess.run([str(exe), str(tmp_path / "ph.bin"), str(tmp_path / "f.bin"), str(tmp_path / "v.bin"), "2"],
+                   check=True, timeout=300)
+    f = np.fromfile(tmp_path / "f.bin", dtype=np.float64).reshape(512, 512)
+    v = np.fromfile(tmp_path / "v.bin", dtype=np.float64).reshape(512, 512)
+    g = oracle.gc_A(ph)
+    fo, vo, _ = oracle.solve(None, g, 1000.0, 0.002, 1e-4, 2, 10, 10)
+    assert np.linalg.norm(f - fo) <= 1e-4 * np.linalg.norm(fo)
+    assert np.linalg.norm(v - vo) <= 1e-4 * np.linalg.norm(vo)

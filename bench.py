@@ -206,6 +206,7 @@ def run_ours(args):
     value = whole_job_rate(args.steps * B, ms / 1e3, world)
     f0, v0 = solver.get(0, stream=st)
     psnr = mg.phantom.psnr(f0, phantoms[0])
+    quality = mg.quality(f0, phantoms[0], dynamic_range=float(phantoms[0].max()))  # on the GPU
     tr = solver.trace(0)
 
     # ---- e2e: host buffers through the C-ABI, copies inside the timed region
@@ -237,6 +238,29 @@ def run_ours(args):
     e2e_s = reduce_max(time.perf_counter() - t0, device="cuda")
     e2e_value = whole_job_rate(args.steps * B, e2e_s, world)
     del fp32
+
+    # ---- linear-mode variant (same slices, redundant forward projections replaced)
+    variants = {}
+    if args.variants and prm.mode == 0:
+        prm_lin = configs.params_for(spec, mode=1)
+        lin = mg.Solver([plan] * B, prm_lin)
+        for b in range(B):
+            lin.set_sino(b, sinos[b])
+        lin.run(stream=st)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(tstream)
+        for _ in range(args.steps):
+            with torch.cuda.stream(tstream):
+                flush.zero_()
+            lin.run(stream=st, sync=False)
+        e1.record(tstream)
+        torch.cuda.synchronize()
+        fl, _ = lin.get(0, stream=st)
+        variants["linear"] = {"value": round(args.steps * B / (e0.elapsed_time(e1) / 1e3), 4), "unit": UNIT,
+                              "psnr_db": round(mg.phantom.psnr(fl, phantoms[0]), 3),
+                              "f_rel_l2_vs_exact": float(np.linalg.norm(fl - f0) / np.linalg.norm(f0))}
+        lin.close()
 
     # ---- roofline: the dominant kernel alone, same workload, CUDA events
     d_img = torch.from_numpy(phantoms[0]).cuda()
@@ -284,6 +308,7 @@ def run_ours(args):
                        "segments_per_projection": S_seg, "projections_per_slice": {"forward": fp_calls, "back": bp_calls}},
             "gsegs_per_s": round(gsegs, 3),
             "psnr_db": round(psnr, 3),
+            "ssim": round(quality["ssim"], 4),
             "exits": [t[:4] for t in tr if t[3] != 0][:6],
             "e2e": {"value": round(e2e_value, 4), "unit": UNIT, "h2d_bytes_per_step": int(B * sinos[0].nbytes),
                     "d2h_bytes_per_step": int(B * 2 * phantoms[0].nbytes)},
@@ -295,6 +320,7 @@ def run_ours(args):
                                          "achieved_gbs": round(v["bytes"] / (v["ms"] / 1e3) / 1e9, 1)}
                                      for k, v in kern.items()}},
             "cpu_baseline": cpu,
+            "variants": variants,
             "serving": serving,
             "clocks": clocks,
             "gpu_launches": int(args.steps * (1 + prm.iter_alt * launches_outer)),
@@ -429,6 +455,7 @@ def main():
     ap.add_argument("--cpu-outer", type=int, default=1, help="outer iterations in the CPU baseline sample")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--serve-requests", type=int, default=12, help="requests in the serving sample (0 = skip)")
+    ap.add_argument("--no-variants", dest="variants", action="store_false", help="skip the linear-mode variant")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

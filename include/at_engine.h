@@ -156,6 +156,16 @@ int at_solver_launches_per_outer(const at_solver *s, int32_t *n);
 int at_reconstruct_host(const at_plan *plan, const at_params *params, const float *h_sino, float *h_f,
                         float *h_v);
 
+/* ---- image quality on the GPU (device buffers, result to the host) ----
+ * PSNR = 10 log10(peak^2 / MSE) as msbeam/CPU_OpenMP/PSNR.m:1-12 computes it
+ * (that script fixes peak = 256); peak <= 0 selects max(ref).
+ * SSIM with the defaults of msbeam/CPU_OpenMP/ssim_index.m: 11x11 Gaussian
+ * window of sigma 1.5, K1 = 0.01, K2 = 0.03, valid window positions, mean of
+ * the map; dynamic_range is its L. */
+int at_psnr(const float *d_x, const float *d_ref, int64_t n, double peak, double *h_psnr, void *stream);
+int at_ssim(const float *d_x, const float *d_ref, int32_t h, int32_t w, double dynamic_range, double *h_ssim,
+            void *stream);
+
 /* ---- continuous-batching server ----
  * Requests are admitted into a running batch once they have arrived and
  * their device state fits the HBM budget and a slot is free; every round

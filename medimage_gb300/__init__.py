@@ -18,9 +18,10 @@ from .engine import (  # noqa: F401
     Solver,
     device_info,
     lib,
+    quality,
     reconstruct,
 )
-from . import configs, phantom  # noqa: F401
+from . import configs, io, phantom  # noqa: F401
 
 __all__ = [
     "AtError",
@@ -30,8 +31,10 @@ __all__ = [
     "Server",
     "Solver",
     "configs",
+    "io",
     "device_info",
     "lib",
     "phantom",
+    "quality",
     "reconstruct",
 ]

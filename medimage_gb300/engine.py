@@ -133,6 +133,9 @@ SIGNATURES = {
     "at_reconstruct_host": ([C.c_void_p, C.POINTER(_Params), _fp, _fp, _fp], C.c_int),
     "at_forward_residual_noalloc": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p],
                                     C.c_int),
+    "at_psnr": ([C.c_void_p, C.c_void_p, C.c_int64, C.c_double, C.POINTER(C.c_double), C.c_void_p], C.c_int),
+    "at_ssim": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_double, C.POINTER(C.c_double), C.c_void_p],
+                C.c_int),
     "at_server_create": ([C.POINTER(_ServerConfig), C.POINTER(C.c_void_p)], C.c_int),
     "at_server_destroy": ([C.c_void_p], None),
     "at_server_submit": ([C.c_void_p, C.c_void_p, _fp, C.c_int32, C.c_double, C.POINTER(C.c_int64)], C.c_int),
@@ -450,3 +453,26 @@ class Server:
         st = _ServerStats()
         _check("at_server_get_stats", lib().at_server_get_stats(self._h, C.byref(st)))
         return {k: getattr(st, k) for k, _ in _ServerStats._fields_}
+
+
+def quality(x: np.ndarray, ref: np.ndarray, peak: float = 0.0, dynamic_range: float | None = None) -> dict:
+    """PSNR (peak <= 0: max(ref)) and SSIM computed on the GPU (at_psnr, at_ssim)."""
+    x = np.ascontiguousarray(x, np.float32)
+    ref = np.ascontiguousarray(ref, np.float32)
+    assert x.shape == ref.shape and x.ndim == 2
+    L = lib()
+    ptrs = []
+    try:
+        for a in (x, ref):
+            p = C.c_void_p()
+            _check("at_dev_alloc", L.at_dev_alloc(C.byref(p), a.nbytes))
+            ptrs.append(p)
+            _check("at_memcpy_h2d", L.at_memcpy_h2d(p, a.ctypes.data, a.nbytes, None))
+        ps, ss = C.c_double(), C.c_double()
+        _check("at_psnr", L.at_psnr(ptrs[0], ptrs[1], x.size, peak, C.byref(ps), None))
+        dr = float(dynamic_range) if dynamic_range else float(ref.max() - min(ref.min(), 0.0)) or 1.0
+        _check("at_ssim", L.at_ssim(ptrs[0], ptrs[1], x.shape[0], x.shape[1], dr, C.byref(ss), None))
+        return {"psnr_db": ps.value, "ssim": ss.value}
+    finally:
+        for p in ptrs:
+            L.at_dev_free(p)

@@ -43,6 +43,7 @@ extern "C" {
 /* geometry kinds */
 #define AT_GEOM_GOLDNC 0 /* GoldenC parallel beam: 512x512, 180 views x 767 detectors */
 #define AT_GEOM_FAN 1    /* 2D fan beam with an equiangular detector                */
+#define AT_GEOM_RAYS 2   /* 2D rays given one by one by their end points            */
 
 /* 2D fan-beam geometry, the parameters of helical/rebin (main.h:16-47,
  * ms2d.cpp:30-62,172-183).  Image n x n, pixel index x*n + y (x slow),
@@ -100,6 +101,14 @@ int at_device_info(char *name, int name_len, int *sm_count, size_t *hbm_bytes);
 /* ---- plans ---- */
 int at_plan_create_fan(const at_fan_geometry *geom, at_plan **out);
 int at_plan_create_goldnc(at_plan **out);
+/* Any 2D geometry as a table of rays: h_endpoints[(view*ndets + det)*4 + 0..3]
+ * = (sx, sy, dx, dy) in mm, the arguments of the reference tracer
+ * forward_proj(sx, sy, dx, dy, ...) (helical/rebin/src/tracing.cpp:22-147);
+ * same image frame as at_fan_geometry (x*n + y, image on [0, n*pixel_mm]^2).
+ * Covers non-uniform view tables (ms2d.cpp:30-62) and parallel beams
+ * (msbeam/CPU_OpenMP/src/proj.c:53-65).  The table is copied. */
+int at_plan_create_rays(int32_t n, double pixel_mm, int32_t nviews, int32_t ndets, const double *h_endpoints,
+                        at_plan **out);
 void at_plan_destroy(at_plan *plan);
 int at_plan_get_stats(const at_plan *plan, at_plan_stats *out);
 /* Traversal of one ray as the device plan stores it: pixel indices and FP32

@@ -12,6 +12,7 @@ from __future__ import annotations
 from .engine import (  # noqa: F401
     AtError,
     FanGeometry,
+    RayGeometry,
     Params,
     Plan,
     Server,
@@ -26,6 +27,7 @@ from . import configs, io, phantom  # noqa: F401
 __all__ = [
     "AtError",
     "FanGeometry",
+    "RayGeometry",
     "Params",
     "Plan",
     "Server",

@@ -36,7 +36,7 @@ struct __align__(16) RayHdr {
   int32_t pix0;   // x0*n + y0 of the first pixel
   int32_t nseg;   // segments the reference's loop emits
   int32_t xy0;    // x0 | (y0 << 16)
-  int32_t sgn;    // bit0: signx > 0, bit1: signy > 0
+  int32_t sgn;    // bit0: signx > 0, bit1: signy > 0, bit2: some segment lies off the grid
   float ax, ay, lenx, leny;
 };
 static_assert(sizeof(RayHdr) == 32, "RayHdr must stay 32 bytes");
@@ -95,7 +95,8 @@ void fan_tables(const at_fan_geometry &g, double *scos, double *ssin, double *dc
 int validate_fan(const at_fan_geometry &g);
 
 // plan construction (plan.cu)
-int build_fan_plan(Plan &p, cudaStream_t st);
+int build_fan_plan(Plan &p, cudaStream_t st, const double *h_ends = nullptr);  // h_ends: [rays][4] for AT_GEOM_RAYS
+int validate_rays(int n, double pixel_mm, int nviews, int ndets, const double *h_ends);
 int build_goldnc_plan(Plan &p, cudaStream_t st);
 int autotune_fan(Plan &p, cudaStream_t st);
 

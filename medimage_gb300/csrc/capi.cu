@@ -124,6 +124,30 @@ AT_API int at_plan_create_fan(const at_fan_geometry *geom, at_plan **out) {
   return AT_OK;
 }
 
+AT_API int at_plan_create_rays(int32_t n, double pixel_mm, int32_t nviews, int32_t ndets, const double *h_endpoints,
+                               at_plan **out) {
+  AT_CHECK_ARG(h_endpoints && out, "at_plan_create_rays: null argument");
+  *out = nullptr;
+  int rc = validate_rays(n, pixel_mm, nviews, ndets, h_endpoints);
+  if (rc) return rc;
+  auto P = std::make_unique<at_plan>();
+  P->p.kind = AT_GEOM_RAYS;
+  P->p.geom = at_fan_geometry{};
+  P->p.geom.n = n;
+  P->p.geom.pixel_mm = pixel_mm;
+  P->p.geom.nviews = nviews;
+  P->p.geom.ndets = ndets;
+  cudaStream_t st;
+  AT_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  rc = build_fan_plan(P->p, st, h_endpoints);
+  if (!rc) rc = autotune_fan(P->p, st);
+  cudaStreamSynchronize(st);
+  cudaStreamDestroy(st);
+  if (rc) return rc;
+  *out = P.release();
+  return AT_OK;
+}
+
 AT_API int at_plan_create_goldnc(at_plan **out) {
   AT_CHECK_ARG(out, "at_plan_create_goldnc: null argument");
   *out = nullptr;

@@ -42,4 +42,23 @@ int validate_fan(const at_fan_geometry &g) {
   return AT_OK;
 }
 
+int validate_rays(int n, double pixel_mm, int nviews, int ndets, const double *h_ends) {
+  if (n < 8 || n > 8191) return set_error(AT_EINVAL, "ray table: n must be in [8, 8191]");
+  if (nviews < 1 || nviews > 65536) return set_error(AT_EINVAL, "ray table: nviews must be in [1, 65536]");
+  if (ndets < 1 || ndets > 49152) return set_error(AT_EINVAL, "ray table: ndets must be in [1, 49152]");
+  if (!(pixel_mm > 0) || !std::isfinite(pixel_mm)) return set_error(AT_EINVAL, "ray table: need pixel_mm > 0");
+  if ((int64_t)nviews * ndets > (1ll << 31) / 2) return set_error(AT_EINVAL, "ray table: too many rays");
+  // the traversal indexes cells as doubles divided by the pixel size; end
+  // points far outside the grid would overflow the int cell index
+  const double lim = 1e6 * n * pixel_mm;
+  for (int64_t r = 0; r < (int64_t)nviews * ndets; r++) {
+    const double *e = h_ends + 4 * r;
+    for (int k = 0; k < 4; k++)
+      if (!std::isfinite(e[k]) || std::fabs(e[k]) > lim)
+        return set_error(AT_EINVAL, "ray table: end point not finite or too far from the grid");
+    if (e[0] == e[2] && e[1] == e[3]) return set_error(AT_EINVAL, "ray table: source and detector coincide");
+  }
+  return AT_OK;
+}
+
 }  // namespace at

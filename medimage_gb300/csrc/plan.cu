@@ -26,20 +26,46 @@ struct FanDevTables {
   const double *scos, *ssin, *dcos, *dsin;
 };
 
+// Where a ray's end points come from: the fan geometry's tables
+// (helical/rebin/src/ms2d.cpp:172-183) or a caller's table of
+// (sx, sy, dx, dy) per ray, the arguments of the reference tracer's
+// forward_proj (helical/rebin/src/tracing.cpp:22).
+struct RaySource {
+  at_fan_geometry g;
+  FanDevTables T;
+  const double *ends;  // [rays][4] for AT_GEOM_RAYS, else null
+};
+
+__device__ __forceinline__ void ray_endpoints(const RaySource &R, int view, int det, double &sx, double &sy,
+                                              double &dx, double &dy) {
+  if (R.ends) {
+    const double *e = R.ends + ((size_t)view * R.g.ndets + det) * 4;
+    sx = e[0];
+    sy = e[1];
+    dx = e[2];
+    dy = e[3];
+    return;
+  }
+  const at_fan_geometry &g = R.g;
+  const double vx = g.pixel_mm, vy = g.pixel_mm;
+  // ms2d.cpp:172-183
+  const double scos = R.T.scos[view], ssin = R.T.ssin[view];
+  const double dcos = R.T.dcos[det], dsin = R.T.dsin[det];
+  sx = g.sod_mm * scos + g.n * vx / 2.0;
+  sy = g.sod_mm * ssin + g.n * vy / 2.0;
+  dx = g.sdd_mm * (dcos * scos - dsin * ssin) + sx;
+  dy = g.sdd_mm * (dsin * scos + dcos * ssin) + sy;
+}
+
 // Traces ray (view, det).  Mode 0: fill the header and count segments.
 // Mode 1: also write the decision words into the block-interleaved array.
 template <int kMode>
-__device__ void fan_trace_ray(const at_fan_geometry g, FanDevTables T, int view, int det, RayHdr *hdr,
-                              int *offgrid, uint32_t *bits, uint32_t word_stride) {
-  const int NX = g.n, NY = g.n;
-  const double vx = g.pixel_mm, vy = g.pixel_mm;
-  // ms2d.cpp:172-183
-  const double scos = T.scos[view], ssin = T.ssin[view];
-  const double dcos = T.dcos[det], dsin = T.dsin[det];
-  const double sx = g.sod_mm * scos + NX * vx / 2.0;
-  const double sy = g.sod_mm * ssin + NX * vy / 2.0;
-  const double dx = g.sdd_mm * (dcos * scos - dsin * ssin) + sx;
-  const double dy = g.sdd_mm * (dsin * scos + dcos * ssin) + sy;
+__device__ void fan_trace_ray(const RaySource &R, int view, int det, RayHdr *hdr, int *offgrid, uint32_t *bits,
+                              uint32_t word_stride) {
+  const int NX = R.g.n, NY = R.g.n;
+  const double vx = R.g.pixel_mm, vy = R.g.pixel_mm;
+  double sx, sy, dx, dy;
+  ray_endpoints(R, view, det, sx, sy, dx, dy);
   // tracing.cpp:39-87
   int index = 0;
   const double ray_x = dx - sx, ray_y = dy - sy;
@@ -128,26 +154,54 @@ __device__ void fan_trace_ray(const at_fan_geometry g, FanDevTables T, int view,
   if (kMode == 1 && (numb & 31) != 0) bits[(size_t)(numb >> 5) * word_stride] = word;
   if (kMode == 0) {
     h.nseg = numb;
+    if (bad) h.sgn |= 4;
     *hdr = h;
     *offgrid = bad;
   }
 }
 
-__global__ void fan_count_kernel(at_fan_geometry g, FanDevTables T, RayHdr *hdr, int *offgrid) {
+__global__ void fan_count_kernel(const RaySource R, RayHdr *hdr, int *offgrid) {
   const int ray = blockIdx.x * blockDim.x + threadIdx.x;
-  if (ray >= g.nviews * g.ndets) return;
-  const int view = ray / g.ndets, det = ray % g.ndets;
-  fan_trace_ray<0>(g, T, view, det, hdr + ray, offgrid + ray, nullptr, 0);
+  if (ray >= R.g.nviews * R.g.ndets) return;
+  const int view = ray / R.g.ndets, det = ray % R.g.ndets;
+  fan_trace_ray<0>(R, view, det, hdr + ray, offgrid + ray, nullptr, 0);
 }
 
-__global__ void fan_fill_kernel(at_fan_geometry g, FanDevTables T, int nblocks_per_view, const uint32_t *blk_word,
-                                uint32_t *bits) {
+__global__ void fan_fill_kernel(const RaySource R, int nblocks_per_view, const uint32_t *blk_word, uint32_t *bits) {
   const int ray = blockIdx.x * blockDim.x + threadIdx.x;
-  if (ray >= g.nviews * g.ndets) return;
-  const int view = ray / g.ndets, det = ray % g.ndets;
+  if (ray >= R.g.nviews * R.g.ndets) return;
+  const int view = ray / R.g.ndets, det = ray % R.g.ndets;
   const int blk = view * nblocks_per_view + det / kRayBlock;
   uint32_t *dst = bits + blk_word[blk] + (det % kRayBlock);
-  fan_trace_ray<1>(g, T, view, det, nullptr, nullptr, dst, kRayBlock);
+  fan_trace_ray<1>(R, view, det, nullptr, nullptr, dst, kRayBlock);
+}
+
+// Segments each pixel receives from each block of kBpViewBlock views, for the
+// back projector's fixed-point range when no geometric bound is known.
+__global__ void pixel_hits_kernel(int n, int view0, int view1, int ndets, int nbpv, const RayHdr *hdr,
+                                  const uint32_t *bits, const uint32_t *blk_word, unsigned *hits) {
+  const int ray = view0 * ndets + blockIdx.x * blockDim.x + threadIdx.x;
+  if (ray >= view1 * ndets) return;
+  const RayHdr h = hdr[ray];
+  const int view = ray / ndets, det = ray % ndets;
+  const uint32_t *wp = bits + blk_word[view * nbpv + det / kRayBlock] + (det % kRayBlock);
+  int x = h.xy0 & 0xffff, y = h.xy0 >> 16;
+  const int sx = (h.sgn & 1) ? 1 : -1, sy = (h.sgn & 2) ? 1 : -1;
+  uint32_t word = 0;
+  for (int k = 0; k < h.nseg; k++) {
+    if ((k & 31) == 0) word = wp[(size_t)(k >> 5) * kRayBlock];
+    if ((unsigned)x < (unsigned)n && (unsigned)y < (unsigned)n) atomicAdd(hits + (size_t)x * n + y, 1u);
+    if ((word >> (k & 31)) & 1u) x += sx;
+    else y += sy;
+  }
+}
+
+__global__ void max_kernel(const unsigned *v, size_t n, unsigned *out) {
+  unsigned m = 0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    m = max(m, v[i]);
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
 }
 
 namespace {
@@ -287,14 +341,39 @@ int build_fan_runs(Plan &p, cudaStream_t st) {
   gather_runs_kernel<<<(int)((tot + 255) / 256) + 1, 256, 0, st>>>(tmp_ent, idx_out, p.run_d, tot);
   AT_CUDA_TRY(cudaGetLastError());
   AT_CUDA_TRY(cudaMemcpyAsync(p.tile_off_d, off.data(), sizeof(int32_t) * (ncell + 1), cudaMemcpyHostToDevice, st));
-  // Contributions one pixel can receive from one view: rays through a pixel are
-  // at least d_min * pitch apart (d_min = closest approach of the image to the
-  // source), so at most ceil(pixel diagonal / that) + 1 of them cross it.
-  const at_fan_geometry &g = p.geom;
-  const double dmin = g.sod_mm - g.n * g.pixel_mm * std::sqrt(2.0) / 2.0;
-  const double spacing = dmin * g.det_pitch_deg * M_PI / 180.0;
-  const int per_view = (int)std::ceil(std::sqrt(2.0) * g.pixel_mm / spacing) + 1;
-  const double per_block = (double)per_view * kBpViewBlock;
+  // Terms one pixel can receive within one view block bound the fixed-point
+  // scale.  Fan beam: rays through a pixel are at least d_min * pitch apart
+  // (d_min = closest approach of the image to the source), so at most
+  // ceil(pixel diagonal / that) + 1 of them cross it per view.  Ray tables: the
+  // exact count, taken from the traversal.
+  double per_block;
+  if (p.kind == AT_GEOM_FAN) {
+    const at_fan_geometry &g = p.geom;
+    const double dmin = g.sod_mm - g.n * g.pixel_mm * std::sqrt(2.0) / 2.0;
+    const double spacing = dmin * g.det_pitch_deg * M_PI / 180.0;
+    const int per_view = (int)std::ceil(std::sqrt(2.0) * g.pixel_mm / spacing) + 1;
+    per_block = (double)per_view * kBpViewBlock;
+  } else {
+    const size_t cells = (size_t)p.n * p.n;
+    unsigned *hits = nullptr, *mx = nullptr;
+    AT_CUDA_TRY(cudaMalloc(&hits, sizeof(unsigned) * (cells + 1)));
+    mx = hits + cells;
+    AT_CUDA_TRY(cudaMemsetAsync(mx, 0, sizeof(unsigned), st));
+    for (int vb = 0; vb < p.nvb; vb++) {
+      const int v0 = vb * kBpViewBlock, v1 = std::min(p.nviews, v0 + kBpViewBlock);
+      AT_CUDA_TRY(cudaMemsetAsync(hits, 0, sizeof(unsigned) * cells, st));
+      pixel_hits_kernel<<<((v1 - v0) * p.ndets + 127) / 128, 128, 0, st>>>(p.n, v0, v1, p.ndets, p.nblocks_per_view,
+                                                                          p.rays_d, p.bits_d, p.blk_word_d, hits);
+      AT_CUDA_TRY(cudaGetLastError());
+      max_kernel<<<256, 256, 0, st>>>(hits, cells, mx);
+      AT_CUDA_TRY(cudaGetLastError());
+    }
+    unsigned m = 0;
+    AT_CUDA_TRY(cudaMemcpyAsync(&m, mx, sizeof(m), cudaMemcpyDeviceToHost, st));
+    AT_CUDA_TRY(cudaStreamSynchronize(st));
+    cudaFree(hits);
+    per_block = std::max(1u, m);
+  }
   // terms stay below 2^22 so the kernel can round them with one FFMA
   p.bp_term_bits = std::min(22, 31 - (int)std::ceil(std::log2(per_block + 1.0)));
   if (p.bp_term_bits < 16) return set_error(AT_EINVAL, "plan: detector far finer than the pixel grid (back projector precision)");
@@ -310,29 +389,38 @@ int build_fan_runs(Plan &p, cudaStream_t st) {
   return AT_OK;
 }
 
-int build_fan_plan(Plan &p, cudaStream_t st) {
+int build_fan_plan(Plan &p, cudaStream_t st, const double *h_ends) {
   const at_fan_geometry &g = p.geom;
   const int nv = g.nviews, nd = g.ndets, nrays = nv * nd;
   p.n = g.n;
   p.nviews = nv;
   p.ndets = nd;
   p.rays = nrays;
-  std::vector<double> scos(nv), ssin(nv), dcos(nd), dsin(nd);
-  fan_tables(g, scos.data(), ssin.data(), dcos.data(), dsin.data());
   double *tab_d = nullptr;
   int rc;
-  AT_CUDA_TRY(cudaMalloc(&tab_d, sizeof(double) * 2 * (nv + nd)));
-  AT_CUDA_TRY(cudaMemcpyAsync(tab_d, scos.data(), sizeof(double) * nv, cudaMemcpyHostToDevice, st));
-  AT_CUDA_TRY(cudaMemcpyAsync(tab_d + nv, ssin.data(), sizeof(double) * nv, cudaMemcpyHostToDevice, st));
-  AT_CUDA_TRY(cudaMemcpyAsync(tab_d + 2 * nv, dcos.data(), sizeof(double) * nd, cudaMemcpyHostToDevice, st));
-  AT_CUDA_TRY(cudaMemcpyAsync(tab_d + 2 * nv + nd, dsin.data(), sizeof(double) * nd, cudaMemcpyHostToDevice, st));
-  FanDevTables T{tab_d, tab_d + nv, tab_d + 2 * nv, tab_d + 2 * nv + nd};
+  RaySource R{};
+  R.g = g;
+  if (h_ends) {
+    AT_CUDA_TRY(cudaMalloc(&tab_d, sizeof(double) * 4 * (size_t)nrays));
+    AT_CUDA_TRY(cudaMemcpyAsync(tab_d, h_ends, sizeof(double) * 4 * (size_t)nrays, cudaMemcpyHostToDevice, st));
+    R.ends = tab_d;
+  } else {
+    std::vector<double> scos(nv), ssin(nv), dcos(nd), dsin(nd);
+    fan_tables(g, scos.data(), ssin.data(), dcos.data(), dsin.data());
+    AT_CUDA_TRY(cudaMalloc(&tab_d, sizeof(double) * 2 * (nv + nd)));
+    AT_CUDA_TRY(cudaMemcpyAsync(tab_d, scos.data(), sizeof(double) * nv, cudaMemcpyHostToDevice, st));
+    AT_CUDA_TRY(cudaMemcpyAsync(tab_d + nv, ssin.data(), sizeof(double) * nv, cudaMemcpyHostToDevice, st));
+    AT_CUDA_TRY(cudaMemcpyAsync(tab_d + 2 * nv, dcos.data(), sizeof(double) * nd, cudaMemcpyHostToDevice, st));
+    AT_CUDA_TRY(cudaMemcpyAsync(tab_d + 2 * nv + nd, dsin.data(), sizeof(double) * nd, cudaMemcpyHostToDevice, st));
+    AT_CUDA_TRY(cudaStreamSynchronize(st));  // the host tables go out of scope
+    R.T = FanDevTables{tab_d, tab_d + nv, tab_d + 2 * nv, tab_d + 2 * nv + nd};
+  }
 
   if ((rc = dev_alloc(&p.rays_d, nrays, p.device_bytes))) return rc;
   int *off_d = nullptr;
   AT_CUDA_TRY(cudaMalloc(&off_d, sizeof(int) * nrays));
   const int tpb = 128;
-  fan_count_kernel<<<(nrays + tpb - 1) / tpb, tpb, 0, st>>>(g, T, p.rays_d, off_d);
+  fan_count_kernel<<<(nrays + tpb - 1) / tpb, tpb, 0, st>>>(R, p.rays_d, off_d);
   AT_CUDA_TRY(cudaGetLastError());
 
   std::vector<RayHdr> hdr(nrays);
@@ -381,7 +469,7 @@ int build_fan_plan(Plan &p, cudaStream_t st) {
   AT_CUDA_TRY(cudaMemcpyAsync(p.blk_word_d, blk_word.data(), sizeof(uint32_t) * (p.nblocks + 1),
                               cudaMemcpyHostToDevice, st));
   AT_CUDA_TRY(cudaMemcpyAsync(p.blk_nw_d, blk_nw.data(), p.nblocks, cudaMemcpyHostToDevice, st));
-  fan_fill_kernel<<<(nrays + tpb - 1) / tpb, tpb, 0, st>>>(g, T, p.nblocks_per_view, p.blk_word_d, p.bits_d);
+  fan_fill_kernel<<<(nrays + tpb - 1) / tpb, tpb, 0, st>>>(R, p.nblocks_per_view, p.blk_word_d, p.bits_d);
   AT_CUDA_TRY(cudaGetLastError());
 
   if ((rc = build_fan_runs(p, st))) return rc;

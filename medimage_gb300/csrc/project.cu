@@ -130,6 +130,7 @@ __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
     int idx[RPT], stx[RPT], sty[RPT], nseg[RPT];
     float ax[RPT], ay[RPT], lx[RPT], ly[RPT], cx[RPT], cy[RPT], prev[RPT], acc[RPT], comp[RPT];
     int my_max = 0;
+    bool any_off = false;
 #pragma unroll
     for (int r = 0; r < RPT; r++) {
       const int det = det0 + r;
@@ -144,6 +145,7 @@ __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
         nseg[r] = (int)h0.y;
         stx[r] = (h0.w & 1u) ? S.n : -S.n;
         sty[r] = (h0.w & 2u) ? 1 : -1;
+        any_off |= (h0.w & 4u) != 0;
         ax[r] = __uint_as_float(h1.x);
         ay[r] = __uint_as_float(h1.y);
         lx[r] = __uint_as_float(h1.z);
@@ -156,8 +158,9 @@ __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
     int my_min = nseg[0];
 #pragma unroll
     for (int r = 1; r < RPT; r++) my_min = min(my_min, nseg[r]);
+    if (any_off) my_min = 0;  // a ray that leaves the grid takes the checked path
     const int nwords = ((int)__reduce_max_sync(0xffffffffu, (unsigned)my_max) + 31) >> 5;
-    const int wfull = S.offgrid ? 0 : (int)(__reduce_min_sync(0xffffffffu, (unsigned)my_min) >> 5);
+    const int wfull = (int)(__reduce_min_sync(0xffffffffu, (unsigned)my_min) >> 5);
     const uint32_t *wp = S.bits + __ldg(S.blk_word + blk) + in_blk;
     for (int w = 0; w < nwords; w++) {
       uint32_t bw[RPT];
@@ -179,8 +182,8 @@ __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
       for (int r = 0; r < RPT; r++) part[r] = 0.f;
       const int base = w << 5;
       if (w < wfull) {
-        // every ray of the warp has 32 segments in this word and (clean plan)
-        // no segment leaves the grid: no per-segment checks
+        // every ray of the warp has 32 segments in this word and none of them
+        // leaves the grid: no per-segment checks
 #pragma unroll
         for (int b = 0; b < 32; b++) {
 #pragma unroll
@@ -546,7 +549,7 @@ namespace at {
 // keeps the fastest (results are bitwise identical across the three).
 int autotune_fan(Plan &p, cudaStream_t st) {
   p.fp_rpt = 1;
-  if (p.kind != AT_GEOM_FAN) return AT_OK;
+  if (p.kind == AT_GEOM_GOLDNC) return AT_OK;
   float *img = nullptr, *sino = nullptr;
   const size_t npix = (size_t)p.n * p.n, nbins = (size_t)p.nviews * p.ndets;
   AT_CUDA_TRY(cudaMallocAsync(&img, npix * sizeof(float), st));

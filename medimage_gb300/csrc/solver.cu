@@ -284,7 +284,8 @@ int Solver::create(const std::vector<Plan *> &pl, const at_params &prm) {
   if (pl.empty()) return set_error(AT_EINVAL, "solver: no scans");
   const int kind = pl[0]->kind;
   for (auto *p : pl)
-    if (p->kind != kind) return set_error(AT_EINVAL, "solver: a batch must hold one geometry kind");
+    if ((p->kind == AT_GEOM_GOLDNC) != (kind == AT_GEOM_GOLDNC))
+      return set_error(AT_EINVAL, "solver: GoldenC plans cannot share a batch with fan-beam or ray-table plans");
   if (prm.iter_image < 2) return set_error(AT_EINVAL, "solver: iter_image must be >= 2 (the reference divides by iter_image/2)");
   if (prm.iter_edge < 1 || prm.iter_alt < 0) return set_error(AT_EINVAL, "solver: iteration counts must be positive");
   if (prm.mode != 0 && prm.mode != 1) return set_error(AT_EINVAL, "solver: mode must be 0 (exact) or 1 (linear)");

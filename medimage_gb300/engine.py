@@ -11,7 +11,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libat_engine.so")
 
-AT_GEOM_GOLDNC, AT_GEOM_FAN = 0, 1
+AT_GEOM_GOLDNC, AT_GEOM_FAN, AT_GEOM_RAYS = 0, 1, 2
 _fp = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
@@ -103,6 +103,7 @@ SIGNATURES = {
     "at_device_info": ([C.c_char_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_size_t)], C.c_int),
     "at_plan_create_fan": ([C.POINTER(_FanGeom), C.POINTER(C.c_void_p)], C.c_int),
     "at_plan_create_goldnc": ([C.POINTER(C.c_void_p)], C.c_int),
+    "at_plan_create_rays": ([C.c_int32, C.c_double, C.c_int32, C.c_int32, _dp, C.POINTER(C.c_void_p)], C.c_int),
     "at_plan_destroy": ([C.c_void_p], None),
     "at_plan_get_stats": ([C.c_void_p, C.POINTER(_PlanStats)], C.c_int),
     "at_plan_trace_ray": ([C.c_void_p, C.c_int32, C.c_int32, _ip, _fp, C.c_int32, C.POINTER(C.c_int32)], C.c_int),
@@ -218,6 +219,70 @@ class FanGeometry:
 
 
 @dataclass
+class RayGeometry:
+    """Any 2D geometry as a table of rays: endpoints[view*ndets + det] =
+    (sx, sy, dx, dy) in mm, the arguments of the reference tracer
+    forward_proj (helical/rebin/src/tracing.cpp:22-147), in the frame of
+    FanGeometry (pixel index x*n + y, image on [0, n*pixel_mm]^2)."""
+
+    n: int
+    pixel_mm: float
+    nviews: int
+    ndets: int
+    endpoints: np.ndarray = field(repr=False, default=None)
+
+    def __post_init__(self):
+        self.endpoints = np.ascontiguousarray(self.endpoints, np.float64).reshape(self.nviews * self.ndets, 4)
+
+    @classmethod
+    def fan_from_view_table(cls, n: int, pixel_mm: float, ndets: int, angle_deg, sod_mm: float = 541.0,
+                            sdd_mm: float = 949.0, det_pitch_deg: float = 0.0,
+                            off_center: float = 0.5) -> "RayGeometry":
+        """Fan beam whose source angles come from a view table (one angle per
+        projection, any spacing), as helical/rebin reads them
+        (ms2d.cpp:30-62) and places source and detector (ms2d.cpp:172-183).
+        The trig goes through the C library like the reference's."""
+        ang = [float(a) for a in np.asarray(angle_deg, np.float64).ravel()]
+        per_rad = det_pitch_deg * math.pi / 180.0
+        half = ndets // 2
+        dets = [((j + off_center) * per_rad + math.pi) for j in range(-half, ndets - half)]
+        dcos = [math.cos(a) for a in dets]
+        dsin = [math.sin(a) for a in dets]
+        out = np.empty((len(ang), ndets, 4), np.float64)
+        for v, a in enumerate(ang):
+            scos, ssin = math.cos(a / 180.0 * math.pi), math.sin(a / 180.0 * math.pi)
+            sx = sod_mm * scos + n * pixel_mm / 2.0
+            sy = sod_mm * ssin + n * pixel_mm / 2.0
+            for j in range(ndets):
+                out[v, j, 0] = sx
+                out[v, j, 1] = sy
+                out[v, j, 2] = sdd_mm * (dcos[j] * scos - dsin[j] * ssin) + sx
+                out[v, j, 3] = sdd_mm * (dsin[j] * scos + dcos[j] * ssin) + sy
+        return cls(n, pixel_mm, len(ang), ndets, out.reshape(-1, 4))
+
+    @classmethod
+    def msbeam_parallel(cls, n: int = 512, nproj: int = 180, nray: int = 768) -> "RayGeometry":
+        """The parallel beam of msbeam/CPU_OpenMP (proj.c:53-65, proto.h:4-6):
+        unit pixels, view k at angle pi*k/nproj (sin and cos rounded to float
+        as there), ray r on the line through t*(-sin, cos), t = r - nray/2,
+        along (cos, sin).  msbeam addresses pixel (ix, iy) as iy*n + ix, so its
+        (x, y) is (y, x) here; each ray is given by two points n units either
+        side of its closest approach to the centre."""
+        out = np.empty((nproj, nray, 4), np.float64)
+        half = n / 2.0
+        for k in range(nproj):
+            sin_t = float(np.float32(math.sin(3.14159265359 / nproj * k)))
+            cos_t = float(np.float32(math.cos(3.14159265359 / nproj * k)))
+            for r in range(nray):
+                t = float(r - nray // 2)
+                mx, my = -sin_t * t + half, cos_t * t + half  # msbeam (x, y) of the closest point
+                px, py = my, mx                                # this frame
+                ux, uy = sin_t, cos_t                          # direction (cos, sin) swapped
+                out[k, r] = (px - n * ux, py - n * uy, px + n * ux, py + n * uy)
+        return cls(n, 1.0, nproj, nray, out.reshape(-1, 4))
+
+
+@dataclass
 class Params:
     """AT weights and iteration counts; defaults are GoldenC's config.h:6-17."""
 
@@ -250,6 +315,13 @@ class Plan:
         h = C.c_void_p()
         g = geom.c()
         _check("at_plan_create_fan", lib().at_plan_create_fan(C.byref(g), C.byref(h)))
+        return cls(h, geom)
+
+    @classmethod
+    def rays(cls, geom: RayGeometry) -> "Plan":
+        h = C.c_void_p()
+        _check("at_plan_create_rays", lib().at_plan_create_rays(geom.n, geom.pixel_mm, geom.nviews, geom.ndets,
+                                                                geom.endpoints, C.byref(h)))
         return cls(h, geom)
 
     @classmethod

@@ -80,3 +80,32 @@ def psnr(x: np.ndarray, ref: np.ndarray, peak: float | None = None) -> float:
     mse = float(np.mean((np.asarray(x, np.float64) - ref) ** 2))
     peak = float(ref.max()) if peak is None else peak
     return float("inf") if mse == 0 else 10.0 * np.log10(peak * peak / mse)
+
+
+def msbeam_phantom() -> np.ndarray:
+    """The built-in test image of msbeam/CPU_OpenMP (main.c:92-181): 512 x 512
+    unit pixels, a disc of 1 (radius 180), four discs of 2, 2.5, 2.25 and 3
+    (radius 30, centres +-80), a ring of 1.25 and two bar patterns of 2.
+    Distances are evaluated in FP32 as there, so the image is bit-identical to
+    the one that program reconstructs."""
+    n = 512
+    f = np.zeros((n, n), np.float32)
+    x = (np.arange(n, dtype=np.float64) - 255.5).astype(np.float32)[:, None]
+    y = (np.arange(n, dtype=np.float64) - 255.5).astype(np.float32)[None, :]
+
+    def dist(cx: float, cy: float) -> np.ndarray:
+        dx = (x - np.float32(cx)).astype(np.float32)
+        dy = (y - np.float32(cy)).astype(np.float32)
+        s = (dx * dx).astype(np.float32) + (dy * dy).astype(np.float32)
+        return np.sqrt(s.astype(np.float64)).astype(np.float32).astype(np.float64)
+
+    for cx, cy, r, val in ((0, 0, 180.0, 1.0), (80, 80, 30.0, 2.0), (-80, 80, 30.0, 2.5), (80, -80, 30.0, 2.25),
+                           (-80, -80, 30.0, 3.0)):
+        f[dist(cx, cy) <= r] = val
+    d = dist(0, 120)
+    f[(d >= 29.0) & (d <= 30.0)] = 1.25
+    for r0 in (165, 340):
+        for p in range(7):
+            c0, c1 = (238, 256) if p % 2 == 0 else (256, 274)
+            f[r0 + 2 * p:r0 + 2 * p + 2, c0:c1] = 2.0
+    return f

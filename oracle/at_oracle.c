@@ -266,6 +266,14 @@ static double fan_det_angle_rad(const or_fan_geom *g, int det) {
 
 void or_fan_endpoints(const or_fan_geom *g, int view, int det, double *sx, double *sy, double *dx,
                       double *dy) {
+    if (g->ends) {
+        const double *e = g->ends + ((int64_t)view * g->ndets + det) * 4;
+        *sx = e[0];
+        *sy = e[1];
+        *dx = e[2];
+        *dy = e[3];
+        return;
+    }
     double sa = fan_source_angle_rad(g, view);
     double da = fan_det_angle_rad(g, det);
     double scos = cos(sa), ssin = sin(sa), dcos = cos(da), dsin = sin(da);

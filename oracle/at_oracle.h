@@ -56,6 +56,11 @@ typedef struct {
     double off_center;    /* OFF_CENTER (detector index offset)               */
     double view0_deg;     /* source angle of view 0                           */
     double view_step_deg; /* source angle increment per view                  */
+    const double *ends;   /* optional [nviews*ndets][4] (sx, sy, dx, dy) table:
+                             when set, rays are taken from it (any 2D geometry,
+                             the arguments of tracing.cpp:22) and the fan
+                             fields above other than n, pixel_mm, nviews and
+                             ndets are unused                                 */
 } or_fan_geom;
 
 /* Source/detector end points of ray (view, det), ms2d.cpp:172-183. */

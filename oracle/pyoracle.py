@@ -24,6 +24,7 @@ GC_N, GC_DETS, GC_VIEWS = 512, 767, 180
 
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_fp32 = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
 
 
 class FanGeom(C.Structure):
@@ -40,6 +41,7 @@ class FanGeom(C.Structure):
         ("off_center", C.c_double),
         ("view0_deg", C.c_double),
         ("view_step_deg", C.c_double),
+        ("ends", C.c_void_p),
     ]
 
 
@@ -94,6 +96,11 @@ def lib() -> C.CDLL:
                                    C.POINTER(Trace), C.c_int]
         L.or_solve.argtypes = [C.POINTER(Projector), _dp, _dp, _dp, C.c_double, C.c_double, C.c_double,
                                C.c_int, C.c_int, C.c_int, C.POINTER(Trace)]
+        L.or_ms_wray.argtypes = [C.c_int, C.c_int, _ip, _fp32]
+        L.or_ms_wray.restype = C.c_int
+        L.or_ms_A.argtypes = [_fp32, _fp32]
+        L.or_ms_solve.argtypes = [_fp32, _fp32, _fp32, C.c_int, C.c_int]
+        L.or_ms_phantom.argtypes = [_fp32]
         L.or_proj_A.argtypes = [C.POINTER(Projector), _dp, _dp]
         L.or_proj_AT.argtypes = [C.POINTER(Projector), _dp, _dp]
         _lib = L
@@ -115,15 +122,24 @@ class Fan:
     off_center: float = 0.5
     view0_deg: float = 0.0
     view_step_deg: float = 0.0
+    ends: np.ndarray | None = None  # [nviews*ndets, 4] ray table (sx, sy, dx, dy)
 
     def c(self) -> FanGeom:
+        ptr = None
+        if self.ends is not None:
+            self.ends = np.ascontiguousarray(self.ends, np.float64)
+            assert self.ends.shape == (self.nviews * self.ndets, 4)
+            ptr = self.ends.ctypes.data
         return FanGeom(self.n, self.pixel_mm, self.nviews, self.ndets, self.sod_mm, self.sdd_mm,
-                       self.det_pitch_deg, self.off_center, self.view0_deg, self.view_step_deg)
+                       self.det_pitch_deg, self.off_center, self.view0_deg, self.view_step_deg, ptr)
 
 
 def fan_from_engine(geom) -> Fan:
     """Build the oracle's fan description from an engine-side geometry object
-    that has the same field names (n, pixel_mm, nviews, ndets, ...)."""
+    that has the same field names (n, pixel_mm, nviews, ndets, ...), or from a
+    ray table (an object with an `endpoints` array)."""
+    if getattr(geom, "endpoints", None) is not None:
+        return Fan(geom.n, geom.pixel_mm, geom.nviews, geom.ndets, ends=geom.endpoints)
     return Fan(geom.n, geom.pixel_mm, geom.nviews, geom.ndets, geom.sod_mm, geom.sdd_mm,
                geom.det_pitch_deg, geom.off_center, geom.view0_deg, geom.view_step_deg)
 
@@ -249,6 +265,31 @@ def medfilt2(img: np.ndarray) -> np.ndarray:
 
 
 # --------------------------------------------------------------------------
+# msbeam/CPU_OpenMP restatement (row-action AT, the OpenMP CPU comparator)
+# --------------------------------------------------------------------------
+MS_N, MS_NPROJ, MS_NRAY = 512, 180, 768
+
+
+def ms_phantom() -> np.ndarray:
+    f = np.zeros((MS_N, MS_N), np.float32)
+    lib().or_ms_phantom(f)
+    return f
+
+
+def ms_A(img: np.ndarray) -> np.ndarray:
+    g = np.zeros((MS_NPROJ, MS_NRAY), np.float32)
+    lib().or_ms_A(g, np.ascontiguousarray(img, np.float32))
+    return g
+
+
+def ms_solve(g: np.ndarray, iters: int = 10, nthreads: int = 0):
+    f = np.zeros((MS_N, MS_N), np.float32)
+    v = np.ones((MS_N, MS_N), np.float32)
+    lib().or_ms_solve(np.ascontiguousarray(g, np.float32), f, v, iters, nthreads)
+    return f, v
+
+
+# --------------------------------------------------------------------------
 # the reference's own sources (oracle/_ref), only where they were built
 # --------------------------------------------------------------------------
 class Ref:
@@ -257,8 +298,8 @@ class Ref:
 
     @staticmethod
     def available() -> bool:
-        return os.path.exists(os.path.join(REF_DIR, "libgoldnc_ref.so")) and os.path.exists(
-            os.path.join(REF_DIR, "libfan_ref.so"))
+        return all(os.path.exists(os.path.join(REF_DIR, f))
+                   for f in ("libgoldnc_ref.so", "libfan_ref.so", "libmsbeam_ref.so"))
 
     def __init__(self):
         self.gc = C.CDLL(os.path.join(REF_DIR, "libgoldnc_ref.so"))
@@ -271,6 +312,9 @@ class Ref:
                                                       C.c_int]
         self.fan.fanref_trace.argtypes = [C.c_int, C.c_double] + [C.c_double] * 4 + [_ip, _dp]
         self.fan.fanref_trace.restype = C.c_int
+        self.ms = C.CDLL(os.path.join(REF_DIR, "libmsbeam_ref.so"))
+        self.ms.msbeam_ref_main.argtypes = [C.c_int, C.POINTER(C.c_char_p)]
+        self.ms.A.argtypes = [_fp32, _fp32]
 
     def A(self, img):
         out = np.zeros((GC_VIEWS, GC_DETS), np.float64)
@@ -305,3 +349,19 @@ class Ref:
         wgt = np.zeros(4 * n + 64, np.float64)
         k = self.fan.fanref_trace(n, px, sx, sy, dx, dy, ind, wgt)
         return ind[:k].copy(), wgt[:k].copy()
+
+
+def ref_msbeam_run(ref: "Ref", nthreads: int, workdir: str):
+    """Runs the reference msbeam program (its own phantom, data and 10 sweeps)
+    in `workdir` (it writes std.dat, g.dat, img.dat, edge.dat there) and
+    returns its final f and v from the library's globals."""
+    cwd = os.getcwd()
+    os.chdir(workdir)
+    try:
+        argv = (C.c_char_p * 2)(b"msbeam", str(nthreads).encode())
+        ref.ms.msbeam_ref_main(2, argv)
+    finally:
+        os.chdir(cwd)
+    f = np.ctypeslib.as_array((C.c_float * (MS_N * MS_N)).in_dll(ref.ms, "f")).reshape(MS_N, MS_N).copy()
+    v = np.ctypeslib.as_array((C.c_float * (MS_N * MS_N)).in_dll(ref.ms, "v")).reshape(MS_N, MS_N).copy()
+    return f, v

@@ -17,7 +17,9 @@ FLAGS = -O2 -D_GNU_SOURCE -ffp-contract=off -fno-fast-math -fPIC
 GOLDNC := $(REF)/origin/GoldenC/src
 FANSRC := $(REF)/helical/rebin/src
 
-all: $(OUT)/libgoldnc_ref.so $(OUT)/libfan_ref.so $(OUT)/goldnc_fast
+MSBEAM := $(REF)/msbeam/CPU_OpenMP/src
+
+all: $(OUT)/libgoldnc_ref.so $(OUT)/libfan_ref.so $(OUT)/goldnc_fast $(OUT)/libmsbeam_ref.so
 
 $(OUT):
 	mkdir -p $(OUT)
@@ -34,6 +36,12 @@ $(OUT)/libfan_ref.so: $(FANSRC)/tracing.cpp $(HERE)ref_shims/fan_ref_shim.cpp | 
 # GoldenC with the reference's own optimisation flags (timing comparator only).
 $(OUT)/goldnc_fast: $(GOLDNC)/main.c $(GOLDNC)/proj.c | $(OUT)
 	$(CC) -O3 -std=c99 -D_GNU_SOURCE -w -funroll-all-loops -ffast-math -I$(GOLDNC) -Dmain=goldnc_ref_main -shared -fPIC -o $(OUT)/libgoldnc_fast.so $(GOLDNC)/main.c $(GOLDNC)/proj.c -lm && touch $@
+
+# msbeam/CPU_OpenMP (main.c, proj.c, utility.c) with main() renamed; its
+# globals f, v, g and MSbeam() are driven from tests.
+$(OUT)/libmsbeam_ref.so: $(MSBEAM)/main.c $(MSBEAM)/proj.c $(MSBEAM)/utility.c | $(OUT)
+	$(CC) $(FLAGS) -std=gnu99 -w -fopenmp -I$(MSBEAM) -Dmain=msbeam_ref_main -shared -o $@ \
+	    $(MSBEAM)/main.c $(MSBEAM)/proj.c $(MSBEAM)/utility.c -lm
 
 clean:
 	rm -rf $(OUT)

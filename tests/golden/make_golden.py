@@ -12,13 +12,19 @@ Fixtures (all inputs are seeded and regenerated by the tests):
   fan.npz     helical/rebin tracing.cpp ray traversals at the C1 and C2 fan
               geometries: full (pixel, weight) lists for sampled rays and
               per-ray digests for many more
+  msbeam.npz  msbeam/CPU_OpenMP: the built-in phantom (from the std.dat the
+              program writes), wray traversals of sampled rays, rows of
+              A(phantom), and digests + crops of f and v after the program's
+              10 sweeps with one thread (deterministic then)
 """
 from __future__ import annotations
 
+import ctypes as C
 import hashlib
 import math
 import os
 import sys
+import tempfile
 
 import numpy as np
 
@@ -122,13 +128,55 @@ def fan(ref: po.Ref) -> dict:
     return out
 
 
+def float_digest(x: np.ndarray) -> str:
+    return hashlib.sha1(np.ascontiguousarray(x, np.float32).tobytes()).hexdigest()
+
+
+MS_RAYS = [(0, 0), (0, 384), (0, 767), (1, 200), (29, 500), (44, 384), (45, 100), (45, 700), (60, 300),
+           (89, 383), (90, 384), (91, 12), (120, 400), (134, 650), (135, 384), (150, 90), (179, 384), (179, 767)]
+
+
+def msbeam(ref: po.Ref) -> dict:
+    out = {}
+    ms = ref.ms
+    ms.wray.argtypes = [C.c_int, C.c_int, po._ip, po._fp32, C.POINTER(C.c_int), C.POINTER(C.c_float)]
+    ms.omp_set_num_threads.argtypes = [C.c_int]
+    ind_all, w_all, off = [], [], [0]
+    for (k, r) in MS_RAYS:
+        line = np.zeros(2048, np.int32)
+        w = np.zeros(2048, np.float32)
+        nb, sn = C.c_int(), C.c_float()
+        ms.wray(k, r, line, w, C.byref(nb), C.byref(sn))
+        ind_all.append(line[: nb.value].copy())
+        w_all.append(w[: nb.value].copy())
+        off.append(off[-1] + nb.value)
+    out["wray_rays"] = np.array(MS_RAYS, np.int32)
+    out["wray_ind"] = np.concatenate(ind_all)
+    out["wray_w"] = np.concatenate(w_all)
+    out["wray_off"] = np.array(off, np.int64)
+    with tempfile.TemporaryDirectory() as tmp:
+        f, v = po.ref_msbeam_run(ref, 1, tmp)
+        ph = np.loadtxt(os.path.join(tmp, "std.dat"), dtype=np.float64).astype(np.float32)
+    out["phantom_digest"] = np.array(float_digest(ph))
+    g = np.zeros(180 * 768, np.float32)
+    ms.A(g, np.ascontiguousarray(ph.ravel()))
+    out["A_rows"] = g.reshape(180, 768)[::15].copy()
+    out["A_digest"] = np.array(float_digest(g))
+    out["f_digest"] = np.array(float_digest(f))
+    out["v_digest"] = np.array(float_digest(v))
+    out["f_crop"] = f[216:296, 216:296].copy()
+    out["v_crop"] = v[216:296, 216:296].copy()
+    return out
+
+
 def main() -> None:
     if not po.Ref.available():
         raise SystemExit("oracle/_ref is not built: run make -f oracle/ref.mk REF=<reference root>")
     ref = po.Ref()
     np.savez_compressed(os.path.join(OUT, "goldnc.npz"), **goldnc(ref))
     np.savez_compressed(os.path.join(OUT, "fan.npz"), **fan(ref))
-    for fn in ("goldnc.npz", "fan.npz"):
+    np.savez_compressed(os.path.join(OUT, "msbeam.npz"), **msbeam(ref))
+    for fn in ("goldnc.npz", "fan.npz", "msbeam.npz"):
         print(fn, os.path.getsize(os.path.join(OUT, fn)))
 
 

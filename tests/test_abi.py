@@ -57,6 +57,22 @@ def test_bad_geometry_rejected_without_device(engine):
         engine.Plan.fan(g)
 
 
+def test_bad_ray_table_rejected_without_device(engine):
+    g = engine.RayGeometry.msbeam_parallel(64, 8, 96)
+    bad = g.endpoints.copy()
+    bad[5, 2] = np.nan
+    with pytest.raises(engine.AtError) as ei:
+        engine.Plan.rays(engine.RayGeometry(64, 1.0, 8, 96, bad))
+    assert ei.value.code == -1 and "finite" in str(ei.value)
+    bad = g.endpoints.copy()
+    bad[7, 2:] = bad[7, :2]
+    with pytest.raises(engine.AtError) as ei:
+        engine.Plan.rays(engine.RayGeometry(64, 1.0, 8, 96, bad))
+    assert "coincide" in str(ei.value)
+    with pytest.raises(engine.AtError):
+        engine.Plan.rays(engine.RayGeometry(4, 1.0, 8, 96, g.endpoints))
+
+
 def test_null_arguments_rejected(engine):
     L = engine.lib()
     assert L.at_plan_get_stats(None, None) == -1

@@ -9,7 +9,8 @@
 //                                        one view) stores word w of ray i at
 //                                        bits[blk_word[b] + w*128 + i]
 //   blk_word: uint32[nblocks+1]         word offset of each 128-ray block
-//   blk_nw  : uint8 [nblocks]           decision words of the block's longest ray
+//   blk_off : uint8 [nblocks]           1 if a ray of the block has segments
+//                                        off the grid (no unchecked fast path)
 // GoldenC plan: traced walks of proj.c as explicit FP32 segments (CSR by
 // (alpha, raynum) pair) plus the transposed list (CSC by pixel) for the gather.
 #pragma once
@@ -36,7 +37,7 @@ struct __align__(16) RayHdr {
   int32_t pix0;   // x0*n + y0 of the first pixel
   int32_t nseg;   // segments the reference's loop emits
   int32_t xy0;    // x0 | (y0 << 16)
-  int32_t sgn;    // bit0: signx > 0, bit1: signy > 0, bit2: some segment lies off the grid
+  int32_t sgn;    // bit0: signx > 0, bit1: signy > 0
   float ax, ay, lenx, leny;
 };
 static_assert(sizeof(RayHdr) == 32, "RayHdr must stay 32 bytes");
@@ -61,13 +62,14 @@ struct Plan {
   RayHdr *rays_d = nullptr;
   uint32_t *bits_d = nullptr;
   uint32_t *blk_word_d = nullptr;
-  uint8_t *blk_nw_d = nullptr;
+  uint8_t *blk_off_d = nullptr;
   int nblocks_per_view = 0, nblocks = 0;
   // back projection: one entry per (ray, 16x16 tile) run of the traversal,
   // grouped by tile, longest runs first.  Entry = {ray, k_in | nk << 14 |
-  // cx_in << 19, word offset of the ray's decision bits, tile-local x | y << 4
-  // | signx << 8 | signy << 9 | previous step was an x-step << 10}: the run
-  // starts at step k_in after cx_in x-crossings and covers nk segments
+  // cx_in << 19, the run's decision bits (bit j = segment k_in + j; a run in a
+  // 16x16 tile has at most 31 segments), tile-local x | y << 4 | signx << 8 |
+  // signy << 9 | previous step was an x-step << 10}: the run starts at step
+  // k_in after cx_in x-crossings and covers nk segments
   uint4 *run_d = nullptr;
   int32_t *tile_off_d = nullptr;  // [ntiles * nvb + 1]: runs of (tile, view block)
   int ntiles_y = 0, ntiles = 0, nvb = 0;

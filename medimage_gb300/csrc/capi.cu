@@ -62,7 +62,17 @@ int project(const Plan &p, bool forward, const float *in, float *out, cudaStream
     const int rpt = projector_rpt(p);
     e = launch_fp(L, p.kind, rpt, fp_ctas(L.single, rpt), st);
   } else {
+    // stream-ordered scratch: calls on other streams never share it
+    const size_t bpb = bp_scratch_bytes(p);
+    void *scratch = nullptr;
+    if (bpb) {
+      AT_CUDA_TRY(cudaMallocAsync(&scratch, bpb, st));
+      AT_CUDA_TRY(cudaMemsetAsync(scratch, 0, bpb, st));
+      carve_bp_scratch(L.single, p, (char *)scratch);
+      L.single.bp_split = bp_split_for(p.ntiles, p.nvb);
+    }
     e = launch_bp(L, p.kind, bp_ctas(L.single), st);
+    if (scratch) cudaFreeAsync(scratch, st);
   }
   if (e != cudaSuccess) return cuda_error(e, forward ? "forward projection launch" : "back projection launch");
   return AT_OK;

@@ -154,7 +154,6 @@ __device__ void fan_trace_ray(const RaySource &R, int view, int det, RayHdr *hdr
   if (kMode == 1 && (numb & 31) != 0) bits[(size_t)(numb >> 5) * word_stride] = word;
   if (kMode == 0) {
     h.nseg = numb;
-    if (bad) h.sgn |= 4;
     *hdr = h;
     *offgrid = bad;
   }
@@ -233,7 +232,7 @@ __global__ void fan_runs_kernel(int n, int nviews, int ndets, int nbpv, const Ra
   int x = h.xy0 & 0xffff, y = h.xy0 >> 16;
   const int sx = (h.sgn & 1) ? 1 : -1, sy = (h.sgn & 2) ? 1 : -1;
   int cx = 0, cur_tile = -1, run_k = 0, run_cx = 0, run_x = 0, run_y = 0, prevx = 0, run_prevx = 0;
-  uint32_t word = 0;
+  uint32_t word = 0, run_bits = 0;  // run_bits: the run's decisions, bit j = segment run_k + j
   auto close_run = [&](int k_end) {
     if (cur_tile < 0) return;
     const int nk = k_end - run_k;
@@ -242,7 +241,7 @@ __global__ void fan_runs_kernel(int n, int nviews, int ndets, int nbpv, const Ra
       atomicAdd(&tile_count[(size_t)cur_tile * nvb + vb], 1);
     } else {
       const unsigned long long pos = atomicAdd(cursor, 1ull);
-      ent[pos] = make_uint4((unsigned)ray, (unsigned)run_k | ((unsigned)nk << 14) | ((unsigned)run_cx << 19), wbase,
+      ent[pos] = make_uint4((unsigned)ray, (unsigned)run_k | ((unsigned)nk << 14) | ((unsigned)run_cx << 19), run_bits,
                             (unsigned)(run_x & 15) | ((unsigned)(run_y & 15) << 4) | ((h.sgn & 1u) << 8) |
                                 (((h.sgn >> 1) & 1u) << 9) | ((unsigned)run_prevx << 10));
       // by tile, then view block, then longest runs first, then ray order
@@ -264,8 +263,11 @@ __global__ void fan_runs_kernel(int n, int nviews, int ndets, int nbpv, const Ra
       run_x = x;
       run_y = y;
       run_prevx = prevx;
+      run_bits = 0;
     }
     const int bit = (word >> (k & 31)) & 1;
+    // a tile run has at most 31 segments (16 + 16 - 1); off-grid stretches are not runs
+    if (cur_tile >= 0) run_bits |= (uint32_t)bit << (k - run_k);
     if (bit) {
       x += sx;
       cx++;
@@ -433,25 +435,26 @@ int build_fan_plan(Plan &p, cudaStream_t st, const double *h_ends) {
   p.nblocks_per_view = (nd + kRayBlock - 1) / kRayBlock;
   p.nblocks = nv * p.nblocks_per_view;
   std::vector<uint32_t> blk_word(p.nblocks + 1);
-  std::vector<uint8_t> blk_nw(p.nblocks);
+  std::vector<uint8_t> blk_off(p.nblocks);
   uint64_t words = 0;
   int64_t segs = 0, bad = 0;
   int maxseg = 0;
   for (int v = 0; v < nv; v++)
     for (int b = 0; b < p.nblocks_per_view; b++) {
-      int mx = 0;
+      int mx = 0, boff = 0;
       for (int d = b * kRayBlock; d < std::min(nd, (b + 1) * kRayBlock); d++) {
         const RayHdr &h = hdr[(size_t)v * nd + d];
         mx = std::max(mx, h.nseg);
         segs += h.nseg;
         bad += off[(size_t)v * nd + d];
+        boff |= off[(size_t)v * nd + d] != 0;
       }
       maxseg = std::max(maxseg, mx);
       const int blk = v * p.nblocks_per_view + b;
       const int nw = (mx + 31) / 32;
       if (nw > 255) return set_error(AT_EINVAL, "ray longer than 8160 segments");
       blk_word[blk] = (uint32_t)words;
-      blk_nw[blk] = (uint8_t)nw;
+      blk_off[blk] = (uint8_t)boff;
       words += (uint64_t)nw * kRayBlock;
     }
   if (words >= (1ull << 32)) return set_error(AT_EINVAL, "plan exceeds 2^32 decision words");
@@ -464,11 +467,11 @@ int build_fan_plan(Plan &p, cudaStream_t st, const double *h_ends) {
   // a ray's last one without a bounds check
   if ((rc = dev_alloc(&p.bits_d, words + kRayBlock, p.device_bytes))) return rc;
   if ((rc = dev_alloc(&p.blk_word_d, p.nblocks + 1, p.device_bytes))) return rc;
-  if ((rc = dev_alloc(&p.blk_nw_d, p.nblocks, p.device_bytes))) return rc;
+  if ((rc = dev_alloc(&p.blk_off_d, p.nblocks, p.device_bytes))) return rc;
   AT_CUDA_TRY(cudaMemsetAsync(p.bits_d, 0, sizeof(uint32_t) * (words + kRayBlock), st));
   AT_CUDA_TRY(cudaMemcpyAsync(p.blk_word_d, blk_word.data(), sizeof(uint32_t) * (p.nblocks + 1),
                               cudaMemcpyHostToDevice, st));
-  AT_CUDA_TRY(cudaMemcpyAsync(p.blk_nw_d, blk_nw.data(), p.nblocks, cudaMemcpyHostToDevice, st));
+  AT_CUDA_TRY(cudaMemcpyAsync(p.blk_off_d, blk_off.data(), p.nblocks, cudaMemcpyHostToDevice, st));
   fan_fill_kernel<<<(nrays + tpb - 1) / tpb, tpb, 0, st>>>(R, p.nblocks_per_view, p.blk_word_d, p.bits_d);
   AT_CUDA_TRY(cudaGetLastError());
 
@@ -702,7 +705,7 @@ Plan::~Plan() {
   cudaFree(rays_d);
   cudaFree(bits_d);
   cudaFree(blk_word_d);
-  cudaFree(blk_nw_d);
+  cudaFree(blk_off_d);
   cudaFree(run_d);
   cudaFree(tile_off_d);
   cudaFree(gc_seg_d);

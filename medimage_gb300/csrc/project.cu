@@ -18,6 +18,7 @@
 // proj.c:225.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 
 #include "solver.h"
@@ -130,7 +131,6 @@ __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
     int idx[RPT], stx[RPT], sty[RPT], nseg[RPT];
     float ax[RPT], ay[RPT], lx[RPT], ly[RPT], cx[RPT], cy[RPT], prev[RPT], acc[RPT], comp[RPT];
     int my_max = 0;
-    bool any_off = false;
 #pragma unroll
     for (int r = 0; r < RPT; r++) {
       const int det = det0 + r;
@@ -145,7 +145,6 @@ __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
         nseg[r] = (int)h0.y;
         stx[r] = (h0.w & 1u) ? S.n : -S.n;
         sty[r] = (h0.w & 2u) ? 1 : -1;
-        any_off |= (h0.w & 4u) != 0;
         ax[r] = __uint_as_float(h1.x);
         ay[r] = __uint_as_float(h1.y);
         lx[r] = __uint_as_float(h1.z);
@@ -158,9 +157,9 @@ __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
     int my_min = nseg[0];
 #pragma unroll
     for (int r = 1; r < RPT; r++) my_min = min(my_min, nseg[r]);
-    if (any_off) my_min = 0;  // a ray that leaves the grid takes the checked path
     const int nwords = ((int)__reduce_max_sync(0xffffffffu, (unsigned)my_max) + 31) >> 5;
-    const int wfull = (int)(__reduce_min_sync(0xffffffffu, (unsigned)my_min) >> 5);
+    // blocks holding a ray that leaves the grid take the checked path throughout
+    const int wfull = __ldg(S.blk_off + blk) ? 0 : (int)(__reduce_min_sync(0xffffffffu, (unsigned)my_min) >> 5);
     const uint32_t *wp = S.bits + __ldg(S.blk_word + blk) + in_blk;
     for (int w = 0; w < nwords; w++) {
       uint32_t bw[RPT];
@@ -246,12 +245,13 @@ __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
 // run of the traversal that crosses the tile, longest first; warps take 32
 // runs at a time and walk them with the forward walk's decision bits and
 // crossing formula, so each segment gets the forward projector's weight
-// bit-for-bit.  Runs are grouped in blocks of 32 views.  Each contribution w*r
-// is scaled to an integer (a power of two per tile, from the largest |r| on
-// its runs, sized so that one view block's contributions to a pixel cannot
+// bit-for-bit.  Runs are grouped in blocks of 64 views.  Each contribution w*r
+// is scaled to an integer (a power of two per scan, from the largest |r| of
+// its sinogram, sized so that one view block's contributions to a pixel cannot
 // overflow 32 bits) and added to a shared-memory 32-bit accumulator; after
 // each view block every thread folds its pixel into an exact 64-bit register
-// sum.  Integer addition is associative, so the result does not depend on the
+// sum.  A tile's view blocks may be split over several CTAs (load balance when
+// a launch has few tiles); their 64-bit sums add exactly in global memory.  Integer addition is associative, so the result does not depend on the
 // order in which lanes, warps or views arrive (deterministic, no float
 // atomics).
 constexpr int kBpPitch = kBpTile + 1;  // padded row pitch of the accumulator
@@ -260,6 +260,26 @@ constexpr int kBpPitch = kBpTile + 1;  // padded row pitch of the accumulator
 constexpr int kBpCopies = 2;
 constexpr int kBpAccWords = kBpTile * kBpPitch;
 
+// max |r| of each scan's input sinogram, in kBpMaxParts partial maxima
+__global__ void __launch_bounds__(256) sino_absmax_kernel(const Launch L) {
+  const int scan = blockIdx.x / kBpMaxParts, part = blockIdx.x % kBpMaxParts;
+  const ScanDev &S = scan_of(L, L.scans ? scan : 0);
+  if (!flow_active(S, L.flow)) return;
+  const float *__restrict__ sino = S.buf[L.in_buf];
+  float m = 0.f;
+  for (int i = part * blockDim.x + threadIdx.x; i < S.nbins; i += kBpMaxParts * blockDim.x)
+    m = fmaxf(m, fabsf(__ldg(sino + i)));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  __shared__ float wm[8];
+  if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); w++) m = fmaxf(m, wm[w]);
+    S.bpmax[part] = m;
+  }
+}
+
 __global__ void __launch_bounds__(256) fan_bp_kernel(const Launch L) {
   const int scan = L.scans ? find_scan(L.prefix, L.nscans, blockIdx.x) : 0;
   const ScanDev &S = scan_of(L, scan);
@@ -267,19 +287,22 @@ __global__ void __launch_bounds__(256) fan_bp_kernel(const Launch L) {
   const int cta0 = L.scans ? __ldg(L.prefix + scan) : 0;
   const int ncta = L.scans ? __ldg(L.prefix + scan + 1) - cta0 : gridDim.x;
   const int local_cta = blockIdx.x - cta0;
-  const int tile = local_cta;
+  const int ntiles = S.ntiles_y * S.ntiles_y;
+  // CTA = (split, tile): split s walks view blocks [s*nvb/split, (s+1)*nvb/split)
+  const int tile = local_cta % ntiles, split = local_cta / ntiles;
+  const int vb0 = split * S.nvb / S.bp_split, vb1 = (split + 1) * S.nvb / S.bp_split;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const bool real = tile < S.ntiles_y * S.ntiles_y;
+  const bool real = split < S.bp_split;
   __shared__ int acc[kBpCopies * kBpAccWords];
   __shared__ float wmax[8];
+  __shared__ int last_split;
   for (int i = threadIdx.x; i < kBpCopies * kBpAccWords; i += blockDim.x) acc[i] = 0;
   int *const my_acc = acc + (lane % kBpCopies) * kBpAccWords;
   const float *__restrict__ sino = S.buf[L.in_buf];
   const int32_t *toff = S.tile_off + (size_t)(real ? tile : 0) * S.nvb;
-  const int e0 = real ? __ldg(toff) : 0, eN = real ? __ldg(toff + S.nvb) : 0;
-  // fixed-point scale from the largest |r| on the tile's runs
-  float m = 0.f;
-  for (int i = e0 + threadIdx.x; i < eN; i += blockDim.x) m = fmaxf(m, fabsf(__ldg(sino + __ldg(&S.run[i].x))));
+  // fixed-point scale from the largest |r| of the scan (the same in every
+  // split of a tile, so split sums add exactly)
+  float m = threadIdx.x < kBpMaxParts ? S.bpmax[threadIdx.x] : 0.f;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
   if (lane == 0) wmax[warp] = m;
@@ -300,22 +323,18 @@ __global__ void __launch_bounds__(256) fan_bp_kernel(const Launch L) {
   constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
   constexpr int kMagicBits = 0x4B400000;
   if (real && m > 0.f) {
-    for (int vb = 0; vb < S.nvb; vb++) {
+    for (int vb = vb0; vb < vb1; vb++) {
       const int b0 = __ldg(toff + vb), b1 = __ldg(toff + vb + 1);
       // two-stage pipeline: the next chunk's dependent loads fly during this walk
       const uint4 kZ = make_uint4(0u, 0u, 0u, 0u);
       int c = b0 + warp * 32;
       uint4 e = (c + lane < b1) ? __ldg(S.run + c + lane) : kZ;
       uint4 h1 = __ldg(reinterpret_cast<const uint4 *>(S.rays + e.x) + 1);
-      const uint32_t *wq = S.bits + e.z + (size_t)((e.y & 0x3fffu) >> 5) * kRayBlock;
-      uint32_t w0 = __ldg(wq), w1 = __ldg(wq + kRayBlock);
       float r0 = __ldg(sino + e.x);
       for (; c < b1; c += blockDim.x) {
         const int cn = c + blockDim.x;
         const uint4 en = (cn + lane < b1) ? __ldg(S.run + cn + lane) : kZ;
         const uint4 h1n = __ldg(reinterpret_cast<const uint4 *>(S.rays + en.x) + 1);
-        const uint32_t *wn = S.bits + en.z + (size_t)((en.y & 0x3fffu) >> 5) * kRayBlock;
-        const uint32_t w0n = __ldg(wn), w1n = __ldg(wn + kRayBlock);
         const float rn = __ldg(sino + en.x);
         const bool valid = c + lane < b1;
         const float rv = r0;
@@ -323,7 +342,7 @@ __global__ void __launch_bounds__(256) fan_bp_kernel(const Launch L) {
         const int cx_in = (int)(e.y >> 19);
         const float ax = __uint_as_float(h1.x), ay = __uint_as_float(h1.y);
         const float lx = __uint_as_float(h1.z), ly = __uint_as_float(h1.w);
-        uint32_t wnd = __funnelshift_r(w0, w1, k_in & 31);
+        uint32_t wnd = e.z;  // the run's decision bits
         const float rs = rv * scale;
         float cxf = (float)cx_in, cyf = (float)(k_in - cx_in);
         float prev = 0.f;
@@ -346,8 +365,6 @@ __global__ void __launch_bounds__(256) fan_bp_kernel(const Launch L) {
         }
         e = en;
         h1 = h1n;
-        w0 = w0n;
-        w1 = w1n;
         r0 = rn;
       }
       __syncthreads();
@@ -361,8 +378,26 @@ __global__ void __launch_bounds__(256) fan_bp_kernel(const Launch L) {
   }
   const int x = (tile / S.ntiles_y) * kBpTile + (threadIdx.x >> 4);
   const int y = (tile % S.ntiles_y) * kBpTile + (threadIdx.x & 15);
+  const bool mine = real && x < S.n && y < S.n;
+  bool finish = real;
+  if (S.bp_split > 1) {
+    // exact integer sums meet in the scan's 64-bit accumulator; the tile's
+    // last split to arrive takes the total (and leaves zeros) and finishes
+    unsigned long long *gacc = S.bp_acc + (size_t)x * S.n + y;
+    if (mine && total != 0) atomicAdd(gacc, (unsigned long long)total);
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last_split = real && atomicAdd(&S.bp_cnt[tile], 1) == S.bp_split - 1;
+    __syncthreads();
+    finish = last_split;
+    if (finish) {
+      __threadfence();
+      total = mine ? (long long)atomicExch(gacc, 0ull) : 0;
+      if (threadIdx.x == 0) S.bp_cnt[tile] = 0;
+    }
+  }
   double s0 = 0.0;
-  if (real && x < S.n && y < S.n) {
+  if (finish && mine) {
     const float val = (float)((double)total * ldexp(1.0, -sexp));
     bp_epilogue(S, L, x, y, val, s0);
   }
@@ -517,7 +552,16 @@ int fp_ctas(const ScanDev &S, int rpt) {
 
 int bp_ctas(const ScanDev &S) {
   if (S.kind == AT_GEOM_GOLDNC) return (kGcN / 8) * (kGcN / 32);
-  return S.ntiles_y * S.ntiles_y;
+  return S.ntiles_y * S.ntiles_y * std::max(1, S.bp_split);
+}
+
+// CTAs per back-projection tile for a launch over `tiles` tiles: enough for
+// about four waves of six 256-thread CTAs per SM (152 SMs), at most one per
+// view block.  Results do not depend on it (split sums are exact integers).
+int bp_split_for(int tiles, int nvb) {
+  constexpr int kTarget = 4 * 6 * 152;
+  int s = (kTarget + tiles - 1) / std::max(1, tiles);
+  return std::max(1, std::min({s, nvb, kBpMaxSplit}));
 }
 
 int pix_ctas(const ScanDev &S) { return ((S.n + 7) / 8) * ((S.n + 31) / 32); }
@@ -536,8 +580,12 @@ cudaError_t launch_fp(const Launch &L, int kind, int rpt, int nctas, cudaStream_
 }
 
 cudaError_t launch_bp(const Launch &L, int kind, int nctas, cudaStream_t st) {
-  if (kind == AT_GEOM_GOLDNC) gc_bp_kernel<<<nctas, 256, 0, st>>>(L);
-  else fan_bp_kernel<<<nctas, 256, 0, st>>>(L);
+  if (kind == AT_GEOM_GOLDNC) {
+    gc_bp_kernel<<<nctas, 256, 0, st>>>(L);
+  } else {
+    sino_absmax_kernel<<<(L.scans ? L.nscans : 1) * kBpMaxParts, 256, 0, st>>>(L);
+    fan_bp_kernel<<<nctas, 256, 0, st>>>(L);
+  }
   return cudaGetLastError();
 }
 

@@ -92,6 +92,7 @@ struct Server {
                                 cudaMemcpyHostToDevice, st));
     AT_CUDA_TRY(cudaMemsetAsync(r->dev.buf[B_F], 0, sizeof(float) * r->dev.npix, st));  // main.c:36
     AT_CUDA_TRY(launch_fill(r->dev.buf[B_V], 1.f, r->dev.npix, st));                   // main.c:37-40
+    if (const size_t bpb = bp_scratch_bytes(*r->plan)) AT_CUDA_TRY(cudaMemsetAsync(r->dev.bp_acc, 0, bpb, st));
     used += r->bytes;
     peak = std::max(peak, used);
     r->state = 1;

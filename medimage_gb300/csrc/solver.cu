@@ -37,7 +37,7 @@ void fill_scan_plan(ScanDev &S, const Plan &p) {
   S.rays = p.rays_d;
   S.bits = p.bits_d;
   S.blk_word = p.blk_word_d;
-  S.blk_nw = p.blk_nw_d;
+  S.blk_off = p.blk_off_d;
   S.run = p.run_d;
   S.tile_off = p.tile_off_d;
   S.ntiles_y = p.ntiles_y;
@@ -57,7 +57,7 @@ enum Family { FAM_FP = 0, FAM_PIX = 1, FAM_SINO = 2, FAM_BP = 3 };
 size_t align_up(size_t x) { return (x + 255) & ~size_t(255); }
 
 struct ScanLayout {
-  size_t img_bytes, sino_bytes, partial_bytes, trace_bytes, total;
+  size_t img_bytes, sino_bytes, partial_bytes, trace_bytes, bp_bytes, total;
 };
 
 ScanLayout layout_of(const Plan &p, int rpt) {
@@ -67,11 +67,13 @@ ScanLayout layout_of(const Plan &p, int rpt) {
   L.sino_bytes = align_up(nbins * sizeof(float));
   ScanDev tmp;
   fill_scan_plan(tmp, p);
+  tmp.bp_split = kBpMaxSplit;  // size the partials for the largest split
   const int maxcta = std::max({fp_ctas(tmp, rpt), bp_ctas(tmp), pix_ctas(tmp), (int)((nbins + 255) / 256)});
   L.partial_bytes = align_up((size_t)maxcta * 4 * sizeof(double));
   L.trace_bytes = align_up((size_t)kTraceCap * 10 * sizeof(double));
+  L.bp_bytes = bp_scratch_bytes(p);
   L.total = L.img_bytes * B_NIMG + L.sino_bytes * (B_NBUF - B_NIMG) + L.partial_bytes + L.trace_bytes +
-            align_up(sizeof(Ctl));
+            L.bp_bytes + align_up(sizeof(Ctl));
   return L;
 }
 }  // namespace
@@ -93,7 +95,25 @@ void carve_scan(ScanDev &S, const Plan &p, int rpt, char *cur) {
   cur += lay.partial_bytes;
   S.trace = (double *)cur;
   cur += lay.trace_bytes;
+  carve_bp_scratch(S, p, cur);
+  cur += lay.bp_bytes;
   S.ctl = (Ctl *)cur;
+}
+
+size_t bp_scratch_bytes(const Plan &p) {
+  if (p.kind == AT_GEOM_GOLDNC) return 0;
+  return align_up(sizeof(unsigned long long) * (size_t)p.n * p.n) + align_up(sizeof(int) * (size_t)p.ntiles) +
+         align_up(sizeof(float) * kBpMaxParts);
+}
+
+void carve_bp_scratch(ScanDev &S, const Plan &p, char *cur) {
+  S.bp_split = 1;
+  if (p.kind == AT_GEOM_GOLDNC) return;
+  S.bp_acc = (unsigned long long *)cur;
+  cur += align_up(sizeof(unsigned long long) * (size_t)p.n * p.n);
+  S.bp_cnt = (int *)cur;
+  cur += align_up(sizeof(int) * (size_t)p.ntiles);
+  S.bpmax = (float *)cur;
 }
 
 Ctl make_ctl(const at_params &prm) {
@@ -130,6 +150,18 @@ int Batch::set(const ScanDev *scans, int n, int kind_, int rpt_, cudaStream_t st
     AT_CUDA_TRY(cudaMalloc(&prefix_d, sizeof(int) * 4 * (cap + 1)));
   }
   nscans = n;
+  // back-projection split from the tiles of the whole launch
+  std::vector<ScanDev> sc(scans, scans + n);
+  if (kind != AT_GEOM_GOLDNC) {
+    int tiles = 0, nvb = 1 << 30;
+    for (const auto &S : sc) {
+      tiles += S.ntiles_y * S.ntiles_y;
+      nvb = std::min(nvb, S.nvb);
+    }
+    const int split = bp_split_for(tiles, nvb);
+    for (auto &S : sc) S.bp_split = split;
+  }
+  scans = sc.data();
   std::vector<int> pref(4 * (n + 1), 0);
   for (int s = 0; s < n; s++) {
     pref[FAM_FP * (n + 1) + s + 1] = pref[FAM_FP * (n + 1) + s] + fp_ctas(scans[s], rpt);

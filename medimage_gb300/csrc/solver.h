@@ -15,6 +15,12 @@ size_t scan_bytes(const Plan &p, int rpt);
 void carve_scan(ScanDev &S, const Plan &p, int rpt, char *mem);
 // control block of a fresh reconstruction
 Ctl make_ctl(const at_params &prm);
+// back-projection scratch of one scan (zero when handed to the kernels, left
+// zero by them) and how it is laid out; bp_split = 1
+size_t bp_scratch_bytes(const Plan &p);
+void carve_bp_scratch(ScanDev &S, const Plan &p, char *mem);
+// CTAs per back-projection tile for a launch over `tiles` tiles
+int bp_split_for(int tiles, int nvb);
 
 // The launch sequence of the AT iteration over a set of scans: one launch per
 // kernel for the whole set, per-scan CTA ranges from prefix tables.

@@ -73,6 +73,8 @@ struct Ctl {
 };
 
 constexpr int kTraceCap = 4096;  // records per scan (10 doubles each)
+constexpr int kBpMaxParts = 64;  // CTAs of the max |r| pass per scan
+constexpr int kBpMaxSplit = 8;   // most CTAs one back-projection tile is split over
 
 struct ScanDev {
   int kind, n, nviews, ndets;
@@ -81,7 +83,7 @@ struct ScanDev {
   const RayHdr *rays;
   const uint32_t *bits;
   const uint32_t *blk_word;
-  const uint8_t *blk_nw;
+  const uint8_t *blk_off;  // per 128-ray block: a ray leaves the grid
   const uint4 *run;          // back-projection runs grouped by 16x16 tile
   const int32_t *tile_off;   // [tile * nvb + view block]
   int ntiles_y, nvb, bp_term_bits;
@@ -91,6 +93,13 @@ struct ScanDev {
   const int32_t *gc_pair_off;
   const GcEntry *gc_ent;
   const int32_t *gc_pix_off;
+  // back-projection scratch: per-part max |r| of the input sinogram, and (when
+  // a tile's view blocks are split over bp_split CTAs) exact 64-bit pixel sums
+  // and per-tile arrival counters, both left zero by the kernel
+  float *bpmax;                // [kBpMaxParts]
+  unsigned long long *bp_acc;  // [npix]
+  int *bp_cnt;                 // [ntiles]
+  int bp_split;                // CTAs per tile (>= 1)
   // state
   float *buf[B_NBUF];
   Ctl *ctl;

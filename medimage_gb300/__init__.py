@@ -11,6 +11,7 @@ from __future__ import annotations
 
 from .engine import (  # noqa: F401
     AtError,
+    ConeGeometry,
     FanGeometry,
     RayGeometry,
     Params,
@@ -26,6 +27,7 @@ from . import configs, io, phantom  # noqa: F401
 
 __all__ = [
     "AtError",
+    "ConeGeometry",
     "FanGeometry",
     "RayGeometry",
     "Params",

@@ -283,6 +283,33 @@ class RayGeometry:
 
 
 @dataclass
+class ConeGeometry:
+    """3D cone beam with a flat detector: the parameters of industry3d
+    (ct3d.h:17-56, tracing.cpp:51-81).  Volume nz x nx x ny voxels
+    (index z*nx*ny + x*ny + y), sinogram [nproj][ndx][ndy].  half_rows and
+    half_cols centre the detector; the reference uses NDX/2 for both."""
+
+    nx: int
+    ny: int
+    nz: int
+    voxel_mm: float
+    nproj: int
+    ndx: int
+    ndy: int
+    pitch_mm: float
+    sod_mm: float
+    sdd_mm: float
+    half_rows: int = -1
+    half_cols: int = -1
+
+    def __post_init__(self):
+        if self.half_rows < 0:
+            self.half_rows = self.ndx // 2
+        if self.half_cols < 0:
+            self.half_cols = self.ndy // 2
+
+
+@dataclass
 class Params:
     """AT weights and iteration counts; defaults are GoldenC's config.h:6-17."""
 

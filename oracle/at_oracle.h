@@ -80,6 +80,29 @@ void or_fan_A(const or_fan_geom *g, double *sino, const double *img, int nthread
 /* Exact transpose of or_fan_A (scatter, per-thread partial images). */
 void or_fan_AT(const or_fan_geom *g, double *img, const double *sino, int nthreads);
 
+/* ---------------- 3D cone beam (industry3d/src/tracing.cpp, or_cone.c) ---- */
+typedef struct {
+    int nx, ny, nz;        /* NX NY NZ; voxel index z*nx*ny + x*ny + y      */
+    float voxel;           /* SAMPLESIZE (mm per voxel)                      */
+    int nproj;             /* NPROJ views over 360 degrees                   */
+    int ndx, ndy;          /* NDX detector rows (z), NDY columns             */
+    float pitch;           /* PIXELSIZE (mm per detector cell)               */
+    float sod, sdd;        /* SOD, SDD (mm)                                  */
+    int half_rows;         /* HALFDET for the row axis (reference: NDX/2)    */
+    int half_cols;         /* HALFDET for the column axis (reference: NDX/2) */
+} or_cone_geom;
+
+float or_cone_theta(const or_cone_geom *g, int view);
+void or_cone_endpoints(const or_cone_geom *g, int view, int row, int col, float *s, float *d);
+/* mark_off: report segments whose voxel lies off the grid as index -1 */
+int or_cone_trace_points(int nx, int ny, int nz, float sx, float sy, float sz, float dx, float dy, float dz,
+                         int64_t *ind, float *wgt, int cap, int mark_off);
+int or_cone_trace(const or_cone_geom *g, int view, int row, int col, int64_t *ind, float *wgt, int cap,
+                  int mark_off);
+int64_t or_cone_count_segments(const or_cone_geom *g, int nthreads);
+void or_cone_A(const or_cone_geom *g, double *sino, const double *vol, int nthreads);
+void or_cone_AT(const or_cone_geom *g, double *vol, const double *sino, int nthreads);
+
 /* ---------------- AT solver (GoldenC main.c restated for any projector) ---- */
 enum { OR_PROJ_GOLDENC = 0, OR_PROJ_FAN = 1 };
 typedef struct {

@@ -25,6 +25,7 @@ GC_N, GC_DETS, GC_VIEWS = 512, 767, 180
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 _fp32 = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+_i64 = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
 
 
 class FanGeom(C.Structure):
@@ -43,6 +44,14 @@ class FanGeom(C.Structure):
         ("view_step_deg", C.c_double),
         ("ends", C.c_void_p),
     ]
+
+
+class ConeGeom(C.Structure):
+    """Mirror of ``or_cone_geom`` (oracle/at_oracle.h)."""
+
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("voxel", C.c_float), ("nproj", C.c_int),
+                ("ndx", C.c_int), ("ndy", C.c_int), ("pitch", C.c_float), ("sod", C.c_float), ("sdd", C.c_float),
+                ("half_rows", C.c_int), ("half_cols", C.c_int)]
 
 
 class Projector(C.Structure):
@@ -101,6 +110,17 @@ def lib() -> C.CDLL:
         L.or_ms_A.argtypes = [_fp32, _fp32]
         L.or_ms_solve.argtypes = [_fp32, _fp32, _fp32, C.c_int, C.c_int]
         L.or_ms_phantom.argtypes = [_fp32]
+        L.or_cone_theta.argtypes = [C.POINTER(ConeGeom), C.c_int]
+        L.or_cone_theta.restype = C.c_float
+        L.or_cone_endpoints.argtypes = [C.POINTER(ConeGeom), C.c_int, C.c_int, C.c_int, _fp32, _fp32]
+        L.or_cone_trace_points.argtypes = [C.c_int] * 3 + [C.c_float] * 6 + [_i64, _fp32, C.c_int, C.c_int]
+        L.or_cone_trace_points.restype = C.c_int
+        L.or_cone_trace.argtypes = [C.POINTER(ConeGeom), C.c_int, C.c_int, C.c_int, _i64, _fp32, C.c_int, C.c_int]
+        L.or_cone_trace.restype = C.c_int
+        L.or_cone_count_segments.argtypes = [C.POINTER(ConeGeom), C.c_int]
+        L.or_cone_count_segments.restype = C.c_int64
+        L.or_cone_A.argtypes = [C.POINTER(ConeGeom), _dp, _dp, C.c_int]
+        L.or_cone_AT.argtypes = [C.POINTER(ConeGeom), _dp, _dp, C.c_int]
         L.or_proj_A.argtypes = [C.POINTER(Projector), _dp, _dp]
         L.or_proj_AT.argtypes = [C.POINTER(Projector), _dp, _dp]
         _lib = L
@@ -265,6 +285,62 @@ def medfilt2(img: np.ndarray) -> np.ndarray:
 
 
 # --------------------------------------------------------------------------
+# 3D cone beam (industry3d/src/tracing.cpp restated)
+# --------------------------------------------------------------------------
+def cone_c(geom) -> ConeGeom:
+    """ConeGeom from an object with the fields nx, ny, nz, voxel_mm, nproj,
+    ndx, ndy, pitch_mm, sod_mm, sdd_mm, half_rows, half_cols."""
+    return ConeGeom(geom.nx, geom.ny, geom.nz, geom.voxel_mm, geom.nproj, geom.ndx, geom.ndy, geom.pitch_mm,
+                    geom.sod_mm, geom.sdd_mm, geom.half_rows, geom.half_cols)
+
+
+def cone_endpoints(geom, view: int, row: int, col: int):
+    s = np.zeros(3, np.float32)
+    d = np.zeros(3, np.float32)
+    g = cone_c(geom)
+    lib().or_cone_endpoints(C.byref(g), view, row, col, s, d)
+    return s, d
+
+
+def cone_trace(geom, view: int, row: int, col: int, mark_off: bool = False):
+    """(voxel index, FP32 weight) of every segment; with mark_off, segments
+    whose voxel lies off the grid have index -1."""
+    cap = 2 * (geom.nx + geom.ny + geom.nz) + 16
+    ind = np.zeros(cap, np.int64)
+    wgt = np.zeros(cap, np.float32)
+    g = cone_c(geom)
+    n = lib().or_cone_trace(C.byref(g), view, row, col, ind, wgt, cap, int(mark_off))
+    return ind[:n].copy(), wgt[:n].copy()
+
+
+def cone_trace_points(nx, ny, nz, s, d):
+    cap = 2 * (nx + ny + nz) + 16
+    ind = np.zeros(cap, np.int64)
+    wgt = np.zeros(cap, np.float32)
+    n = lib().or_cone_trace_points(nx, ny, nz, *[float(x) for x in s], *[float(x) for x in d], ind, wgt, cap, 0)
+    return ind[:n].copy(), wgt[:n].copy()
+
+
+def cone_segments(geom, nthreads: int = 0) -> int:
+    g = cone_c(geom)
+    return int(lib().or_cone_count_segments(C.byref(g), nthreads))
+
+
+def cone_A(geom, vol: np.ndarray, nthreads: int = 0) -> np.ndarray:
+    out = np.zeros((geom.nproj, geom.ndx, geom.ndy), np.float64)
+    g = cone_c(geom)
+    lib().or_cone_A(C.byref(g), out, np.ascontiguousarray(vol, np.float64), nthreads)
+    return out
+
+
+def cone_AT(geom, sino: np.ndarray, nthreads: int = 0) -> np.ndarray:
+    out = np.zeros((geom.nz, geom.nx, geom.ny), np.float64)
+    g = cone_c(geom)
+    lib().or_cone_AT(C.byref(g), out, np.ascontiguousarray(sino, np.float64), nthreads)
+    return out
+
+
+# --------------------------------------------------------------------------
 # msbeam/CPU_OpenMP restatement (row-action AT, the OpenMP CPU comparator)
 # --------------------------------------------------------------------------
 MS_N, MS_NPROJ, MS_NRAY = 512, 180, 768
@@ -299,7 +375,7 @@ class Ref:
     @staticmethod
     def available() -> bool:
         return all(os.path.exists(os.path.join(REF_DIR, f))
-                   for f in ("libgoldnc_ref.so", "libfan_ref.so", "libmsbeam_ref.so"))
+                   for f in ("libgoldnc_ref.so", "libfan_ref.so", "libmsbeam_ref.so", "libcone_ref.so"))
 
     def __init__(self):
         self.gc = C.CDLL(os.path.join(REF_DIR, "libgoldnc_ref.so"))
@@ -312,6 +388,11 @@ class Ref:
                                                       C.c_int]
         self.fan.fanref_trace.argtypes = [C.c_int, C.c_double] + [C.c_double] * 4 + [_ip, _dp]
         self.fan.fanref_trace.restype = C.c_int
+        self.cone = C.CDLL(os.path.join(REF_DIR, "libcone_ref.so"))
+        self.cone.coneref_endpoints.argtypes = [C.c_int] * 3 + [C.c_float] + [C.c_int] * 3 + [C.c_float] * 3 + \
+            [C.c_int] * 3 + [_fp32, _fp32]
+        self.cone.coneref_trace.argtypes = [C.c_int] * 3 + [C.c_float] * 6 + [_i64, _fp32]
+        self.cone.coneref_trace.restype = C.c_int
         self.ms = C.CDLL(os.path.join(REF_DIR, "libmsbeam_ref.so"))
         self.ms.msbeam_ref_main.argtypes = [C.c_int, C.POINTER(C.c_char_p)]
         self.ms.A.argtypes = [_fp32, _fp32]
@@ -365,3 +446,19 @@ def ref_msbeam_run(ref: "Ref", nthreads: int, workdir: str):
     f = np.ctypeslib.as_array((C.c_float * (MS_N * MS_N)).in_dll(ref.ms, "f")).reshape(MS_N, MS_N).copy()
     v = np.ctypeslib.as_array((C.c_float * (MS_N * MS_N)).in_dll(ref.ms, "v")).reshape(MS_N, MS_N).copy()
     return f, v
+
+
+def ref_cone_endpoints(ref: "Ref", geom, view: int, row: int, col: int):
+    s = np.zeros(3, np.float32)
+    d = np.zeros(3, np.float32)
+    ref.cone.coneref_endpoints(geom.nx, geom.ny, geom.nz, geom.voxel_mm, geom.nproj, geom.ndx, geom.ndy,
+                               geom.pitch_mm, geom.sod_mm, geom.sdd_mm, view, row, col, s, d)
+    return s, d
+
+
+def ref_cone_trace_points(ref: "Ref", nx, ny, nz, s, d):
+    cap = 4 * (nx + ny + nz) + 16  # the reference writes without a bound
+    ind = np.zeros(cap, np.int64)
+    wgt = np.zeros(cap, np.float32)
+    n = ref.cone.coneref_trace(nx, ny, nz, *[float(x) for x in s], *[float(x) for x in d], ind, wgt)
+    return ind[:n].copy(), wgt[:n].copy()

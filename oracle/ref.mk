@@ -19,7 +19,10 @@ FANSRC := $(REF)/helical/rebin/src
 
 MSBEAM := $(REF)/msbeam/CPU_OpenMP/src
 
-all: $(OUT)/libgoldnc_ref.so $(OUT)/libfan_ref.so $(OUT)/goldnc_fast $(OUT)/libmsbeam_ref.so
+CONESRC := $(REF)/industry3d/src
+CONEINC := $(REF)/industry3d/include
+
+all: $(OUT)/libgoldnc_ref.so $(OUT)/libfan_ref.so $(OUT)/goldnc_fast $(OUT)/libmsbeam_ref.so $(OUT)/libcone_ref.so
 
 $(OUT):
 	mkdir -p $(OUT)
@@ -42,6 +45,12 @@ $(OUT)/goldnc_fast: $(GOLDNC)/main.c $(GOLDNC)/proj.c | $(OUT)
 $(OUT)/libmsbeam_ref.so: $(MSBEAM)/main.c $(MSBEAM)/proj.c $(MSBEAM)/utility.c | $(OUT)
 	$(CC) $(FLAGS) -std=gnu99 -w -fopenmp -I$(MSBEAM) -Dmain=msbeam_ref_main -shared -o $@ \
 	    $(MSBEAM)/main.c $(MSBEAM)/proj.c $(MSBEAM)/utility.c -lm
+
+# industry3d's cone geometry and 3D tracer (tracing.cpp, utility.cpp unchanged;
+# utility.cpp includes a Boost header it does not use, stood in by an empty one)
+$(OUT)/libcone_ref.so: $(CONESRC)/tracing.cpp $(CONESRC)/utility.cpp $(HERE)ref_shims/cone_ref_shim.cpp | $(OUT)
+	$(CXX) $(FLAGS) -std=c++14 -w -I$(CONEINC) -I$(HERE)ref_shims/include -shared -o $@ \
+	    $(CONESRC)/tracing.cpp $(CONESRC)/utility.cpp $(HERE)ref_shims/cone_ref_shim.cpp -lm
 
 clean:
 	rm -rf $(OUT)

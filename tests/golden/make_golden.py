@@ -12,6 +12,9 @@ Fixtures (all inputs are seeded and regenerated by the tests):
   fan.npz     helical/rebin tracing.cpp ray traversals at the C1 and C2 fan
               geometries: full (pixel, weight) lists for sampled rays and
               per-ray digests for many more
+  cone.npz    industry3d cone() end points and forward_proj traversals
+              (voxel indices and FP32 weights, bit patterns) for sampled
+              rays of a small cone geometry and of the C4 geometry
   msbeam.npz  msbeam/CPU_OpenMP: the built-in phantom (from the std.dat the
               program writes), wray traversals of sampled rays, rows of
               A(phantom), and digests + crops of f and v after the program's
@@ -31,7 +34,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 sys.path.insert(0, ROOT)
 
-from medimage_gb300.engine import FanGeometry  # noqa: E402
+from medimage_gb300.engine import ConeGeometry, FanGeometry  # noqa: E402
 from medimage_gb300.phantom import ellipse_phantom  # noqa: E402
 from oracle import pyoracle as po  # noqa: E402
 
@@ -169,6 +172,37 @@ def msbeam(ref: po.Ref) -> dict:
     return out
 
 
+CONE_GEOMS = {
+    "small": ConeGeometry(64, 64, 48, 0.4, 90, 64, 64, 0.7, 60.0, 100.0),
+    "c4": ConeGeometry(512, 512, 512, 0.2, 720, 768, 1024, 0.4, 600.0, 1000.0, 384, 384),
+}
+
+
+def cone(ref: po.Ref) -> dict:
+    """Reference end points and traversals.  The reference centres both
+    detector axes at NDX/2 (ct3d.cpp:90), so the C4 entry, whose detector is
+    not square (768 rows x 1024 columns), uses NDX/2 = 384 on both axes."""
+    out = {}
+    for name, g in CONE_GEOMS.items():
+        rng = np.random.default_rng(31)
+        rays = [(0, g.ndx // 2, g.ndy // 2), (g.nproj // 4, 0, 0), (g.nproj // 2, g.ndx - 1, g.ndy - 1)]
+        rays += [(int(rng.integers(g.nproj)), int(rng.integers(g.ndx)), int(rng.integers(g.ndy))) for _ in range(60)]
+        ends, ind_all, w_all, off = [], [], [], [0]
+        for (v, r, c) in rays:
+            s, d = po.ref_cone_endpoints(ref, g, v, r, c)
+            ind, wgt = po.ref_cone_trace_points(ref, g.nx, g.ny, g.nz, s, d)
+            ends.append(np.concatenate([s, d]))
+            ind_all.append(ind)
+            w_all.append(wgt)
+            off.append(off[-1] + ind.size)
+        out[f"{name}_rays"] = np.array(rays, np.int32)
+        out[f"{name}_ends"] = np.array(ends, np.float32)
+        out[f"{name}_ind"] = np.concatenate(ind_all).astype(np.int64)
+        out[f"{name}_w"] = np.concatenate(w_all).astype(np.float32)
+        out[f"{name}_off"] = np.array(off, np.int64)
+    return out
+
+
 def main() -> None:
     if not po.Ref.available():
         raise SystemExit("oracle/_ref is not built: run make -f oracle/ref.mk REF=<reference root>")
@@ -176,7 +210,8 @@ def main() -> None:
     np.savez_compressed(os.path.join(OUT, "goldnc.npz"), **goldnc(ref))
     np.savez_compressed(os.path.join(OUT, "fan.npz"), **fan(ref))
     np.savez_compressed(os.path.join(OUT, "msbeam.npz"), **msbeam(ref))
-    for fn in ("goldnc.npz", "fan.npz", "msbeam.npz"):
+    np.savez_compressed(os.path.join(OUT, "cone.npz"), **cone(ref))
+    for fn in ("goldnc.npz", "fan.npz", "msbeam.npz", "cone.npz"):
         print(fn, os.path.getsize(os.path.join(OUT, fn)))
 
 

@@ -44,6 +44,7 @@ extern "C" {
 #define AT_GEOM_GOLDNC 0 /* GoldenC parallel beam: 512x512, 180 views x 767 detectors */
 #define AT_GEOM_FAN 1    /* 2D fan beam with an equiangular detector                */
 #define AT_GEOM_RAYS 2   /* 2D rays given one by one by their end points            */
+#define AT_GEOM_CONE 3   /* 3D cone beam with a flat detector (industry3d)          */
 
 /* 2D fan-beam geometry, the parameters of helical/rebin (main.h:16-47,
  * ms2d.cpp:30-62,172-183).  Image n x n, pixel index x*n + y (x slow),
@@ -63,6 +64,26 @@ typedef struct at_fan_geometry {
     double view0_deg;
     double view_step_deg;
 } at_fan_geometry;
+
+/* 3D cone-beam geometry, the parameters of industry3d (ct3d.h:17-56,
+ * ct3d.cpp:49-77) with its cone() of tracing.cpp:51-81: volume nz x nx x ny
+ * voxels of voxel_mm (SAMPLESIZE), voxel index z*nx*ny + x*ny + y; view a of
+ * nproj at 2*pi*a/nproj about the z axis, source at distance sod_mm (SOD),
+ * flat detector of ndx rows (z) x ndy columns of pitch_mm (PIXELSIZE) at
+ * sdd_mm (SDD) from the source; cell (row, col) centred at
+ * ((col - half_cols + 0.5)*pitch, (half_rows - row - 0.5)*pitch).  The
+ * reference sets both half widths to NDX/2 (ct3d.cpp:90); they are separate
+ * here so non-square detectors are centred.  Sinogram [nproj][ndx][ndy].
+ * The engine needs nx == ny. */
+typedef struct at_cone_geometry {
+    int32_t nx, ny, nz;
+    float voxel_mm;
+    int32_t nproj;
+    int32_t ndx, ndy;
+    float pitch_mm;
+    float sod_mm, sdd_mm;
+    int32_t half_rows, half_cols;
+} at_cone_geometry;
 
 /* AT functional weights and iteration counts (config.h:6-8,15-17).
  * mode 0 ("exact") makes every projection the reference makes (29 forward and
@@ -93,6 +114,7 @@ typedef struct at_plan_stats {
     int32_t max_segments;  /* longest ray                                      */
     int32_t fp_rays_per_thread; /* forward-projector variant the autotuner chose */
     int64_t bp_runs;       /* (ray, 16x16 tile) runs the back projector walks   */
+    int32_t nz;            /* image slices (1 for 2D plans)                      */
 } at_plan_stats;
 
 const char *at_last_error(void);
@@ -101,6 +123,9 @@ int at_device_info(char *name, int name_len, int *sm_count, size_t *hbm_bytes);
 /* ---- plans ---- */
 int at_plan_create_fan(const at_fan_geometry *geom, at_plan **out);
 int at_plan_create_goldnc(at_plan **out);
+/* 3D cone beam, traced on the fly with the reference's FP32 walk
+ * (industry3d/src/tracing.cpp:123-307); nothing per ray is stored. */
+int at_plan_create_cone(const at_cone_geometry *geom, at_plan **out);
 /* Any 2D geometry as a table of rays: h_endpoints[(view*ndets + det)*4 + 0..3]
  * = (sx, sy, dx, dy) in mm, the arguments of the reference tracer
  * forward_proj(sx, sy, dx, dy, ...) (helical/rebin/src/tracing.cpp:22-147);

@@ -55,6 +55,11 @@ struct Plan {
   int kind = AT_GEOM_FAN;
   at_fan_geometry geom{};
   int n = 0, nviews = 0, ndets = 0;
+  int nz = 1;  // image slices (a cone-beam volume has nz > 1)
+  // cone beam: the geometry and, per view, cos and sin of its angle (FP32,
+  // from the host libm as in the reference's rotate_2d)
+  at_cone_geometry cone{};
+  float2 *cone_trig_d = nullptr;
   int64_t rays = 0, segments = 0, offgrid = 0, device_bytes = 0;
   int max_segments = 0;
   int fp_rpt = 1;  // rays per thread of the forward projector (autotuned)
@@ -95,6 +100,10 @@ int cuda_error(cudaError_t e, const char *what);
 // host-side geometry tables with the reference's libm expressions
 void fan_tables(const at_fan_geometry &g, double *scos, double *ssin, double *dcos, double *dsin);
 int validate_fan(const at_fan_geometry &g);
+int validate_cone(const at_cone_geometry &g);
+void cone_trig(const at_cone_geometry &g, float2 *trig);  // per view (cos, sin)
+int build_cone_plan(Plan &p, cudaStream_t st);
+int cone_trace_ray(const Plan &p, int64_t ray, int32_t *h_pix, float *h_w, int32_t cap, int32_t *n_out);
 
 // plan construction (plan.cu)
 int build_fan_plan(Plan &p, cudaStream_t st, const double *h_ends = nullptr);  // h_ends: [rays][4] for AT_GEOM_RAYS

@@ -2,7 +2,10 @@
 // (origin/GoldenC/src/main.c:81-390) for a batch of scans.
 //
 // Pixel passes use 8 x 32 tiles (x rows, y columns; 256 threads), the same
-// CTA numbering as the back projector, so one prefix table serves both.  Each
+// CTA numbering as the back projector, so one prefix table serves both; a
+// volume (nz > 1 slices, the cone beam) has the tiles of each slice in turn.
+// On volumes the stencils gain the z neighbours (gradients, Laplacian,
+// smoothness energy); the median stays GoldenC's 3x3 within each slice.  Each
 // pass fuses the elementwise update with the reductions the next scalar step
 // needs; neighbours of freshly computed values are recomputed from their
 // inputs instead of being re-read, so no pass waits on another one.
@@ -13,17 +16,20 @@
 namespace at {
 
 struct PixCoord {
-  int x, y, i;
+  int x, y, z, i, base;  // base: index of the slice's first pixel
   bool inside;
 };
 
 __device__ __forceinline__ PixCoord pix_of(int n, int local_cta) {
-  const int tiles_y = (n + 31) >> 5;
+  const int tiles_y = (n + 31) >> 5, tiles = ((n + 7) >> 3) * tiles_y;
   PixCoord c;
-  c.x = (local_cta / tiles_y) * 8 + (threadIdx.x >> 5);
-  c.y = (local_cta % tiles_y) * 32 + (threadIdx.x & 31);
+  c.z = local_cta / tiles;
+  const int t = local_cta % tiles;
+  c.x = (t / tiles_y) * 8 + (threadIdx.x >> 5);
+  c.y = (t % tiles_y) * 32 + (threadIdx.x & 31);
   c.inside = c.x < n && c.y < n;
-  c.i = c.x * n + c.y;
+  c.base = c.z * n * n;
+  c.i = c.base + c.x * n + c.y;
   return c;
 }
 
@@ -93,7 +99,7 @@ __global__ void __launch_bounds__(256) upd_kernel(const Launch L) {
           const int xx = c.x + dx, yy = c.y + dy;
           float val = 0.f;
           if (xx >= 0 && xx < n && yy >= 0 && yy < n) {
-            const int j = xx * n + yy;
+            const int j = c.base + xx * n + yy;
             val = fmaf(c1, p[j], u[j]);
           }
           w[dx + 1][dy + 1] = val;
@@ -130,7 +136,13 @@ __global__ void __launch_bounds__(256) pp_kernel(const Launch L) {
     const double vv = (double)v[c.i];
     const double eps = S.ctl->eps;
     const double a = (double)pc - pu, b = (double)pc - pl;
-    sums[0] = (vv * vv + 0.01 * eps * eps) * (a * a + b * b);
+    if (S.nz == 1) {
+      sums[0] = (vv * vv + 0.01 * eps * eps) * (a * a + b * b);
+    } else {
+      const float pf = c.z > 0 ? pnew(c.i - n * n) : 0.f;
+      const double cz = (double)pc - pf;
+      sums[0] = (vv * vv + 0.01 * eps * eps) * (a * a + b * b + cz * cz);
+    }
     sums[1] = (double)pc * (double)dc;
   }
   reduce_and_finalize<2>(S, L, sums, local_cta, ncta);
@@ -153,7 +165,14 @@ __global__ void __launch_bounds__(256) edge_init_kernel(const Launch L) {
   const float fd = c.x + 1 < n ? f[c.i + n] : 0.f, fu = c.x > 0 ? f[c.i - n] : 0.f;
   const float fr = c.y + 1 < n ? f[c.i + 1] : 0.f, fl = c.y > 0 ? f[c.i - 1] : 0.f;
   const float gx = 0.5f * (fd - fu), gy = 0.5f * (fr - fl);
-  S.buf[B_NN][c.i] = gx * gx + gy * gy;
+  if (S.nz == 1) {
+    S.buf[B_NN][c.i] = gx * gx + gy * gy;
+  } else {
+    const int nn = n * n;
+    const float fb = c.z + 1 < S.nz ? f[c.i + nn] : 0.f, ff = c.z > 0 ? f[c.i - nn] : 0.f;
+    const float gz = 0.5f * (fb - ff);
+    S.buf[B_NN][c.i] = gx * gx + gy * gy + gz * gz;
+  }
 }
 
 // d = -(alpha v n - beta eps lap/4 v + beta (v-1)/(4 eps)), v one-padded
@@ -168,7 +187,7 @@ __global__ void __launch_bounds__(256) edge_d_kernel(const Launch L) {
   const float alpha = (float)ct->alpha, beq = (float)(ct->beta * ct->eps);
   const float b4 = (float)(ct->beta / (4 * ct->eps));
   double sums[3] = {0.0, 0.0, 0.0};
-  if (c.inside) {
+  if (c.inside && S.nz == 1) {
     auto vat = [&](int xx, int yy) -> float {
       return (xx >= 0 && xx < n && yy >= 0 && yy < n) ? v[xx * n + yy] : 1.f;
     };
@@ -187,6 +206,30 @@ __global__ void __launch_bounds__(256) edge_d_kernel(const Launch L) {
     const double gx = 0.5 * ((double)dat(c.x + 1, c.y) - (double)dat(c.x - 1, c.y));
     const double gy = 0.5 * ((double)dat(c.x, c.y + 1) - (double)dat(c.x, c.y - 1));
     sums[2] = gx * gx + gy * gy;
+  } else if (c.inside) {
+    // volumes: six-neighbour Laplacian scaled by 1/6, central differences in z
+    const int nz = S.nz;
+    auto vat = [&](int zz, int xx, int yy) -> float {
+      return (zz >= 0 && zz < nz && xx >= 0 && xx < n && yy >= 0 && yy < n) ? v[(zz * n + xx) * n + yy] : 1.f;
+    };
+    auto dat = [&](int zz, int xx, int yy) -> float {
+      if (zz < 0 || zz >= nz || xx < 0 || xx >= n || yy < 0 || yy >= n) return 0.f;
+      const int j = (zz * n + xx) * n + yy;
+      const float vc = v[j];
+      const float lap = (1.f / 6.f) * (vat(zz, xx + 1, yy) + vat(zz, xx, yy + 1) + vat(zz + 1, xx, yy) - 6.f * vc +
+                                      vat(zz, xx - 1, yy) + vat(zz, xx, yy - 1) + vat(zz - 1, xx, yy));
+      const float g = alpha * vc * nn[j] - beq * lap + b4 * (vc - 1.f);
+      return -g;
+    };
+    const float dc = dat(c.z, c.x, c.y);
+    S.buf[B_D][c.i] = dc;
+    const double dd = (double)dc * dc;
+    sums[0] = dd;
+    sums[1] = (double)nn[c.i] * dd;
+    const double gx = 0.5 * ((double)dat(c.z, c.x + 1, c.y) - (double)dat(c.z, c.x - 1, c.y));
+    const double gy = 0.5 * ((double)dat(c.z, c.x, c.y + 1) - (double)dat(c.z, c.x, c.y - 1));
+    const double gz = 0.5 * ((double)dat(c.z + 1, c.x, c.y) - (double)dat(c.z - 1, c.x, c.y));
+    sums[2] = gx * gx + gy * gy + gz * gz;
   }
   reduce_and_finalize<3>(S, L, sums, local_cta, ncta);
 }

@@ -16,7 +16,8 @@ namespace at {
 int fp_ctas(const ScanDev &S, int rpt);
 int bp_ctas(const ScanDev &S);
 cudaError_t launch_fp(const Launch &L, int kind, int rpt, int nctas, cudaStream_t st);
-cudaError_t launch_bp(const Launch &L, int kind, int nctas, cudaStream_t st);
+cudaError_t launch_bp(const Launch &L, int kind, int nctas, cudaStream_t st, const Launch *Lpix, int pix_nctas);
+int pix_ctas(const ScanDev &S);
 cudaError_t launch_median(const float *in, float *out, int n, cudaStream_t st);
 
 namespace {
@@ -71,7 +72,7 @@ int project(const Plan &p, bool forward, const float *in, float *out, cudaStream
       carve_bp_scratch(L.single, p, (char *)scratch);
       L.single.bp_split = bp_split_for(p.ntiles, p.nvb);
     }
-    e = launch_bp(L, p.kind, bp_ctas(L.single), st);
+    e = launch_bp(L, p.kind, bp_ctas(L.single), st, &L, pix_ctas(L.single));
     if (scratch) cudaFreeAsync(scratch, st);
   }
   if (e != cudaSuccess) return cuda_error(e, forward ? "forward projection launch" : "back projection launch");
@@ -158,6 +159,28 @@ AT_API int at_plan_create_rays(int32_t n, double pixel_mm, int32_t nviews, int32
   return AT_OK;
 }
 
+AT_API int at_plan_create_cone(const at_cone_geometry *geom, at_plan **out) {
+  AT_CHECK_ARG(geom && out, "at_plan_create_cone: null argument");
+  *out = nullptr;
+  int rc = validate_cone(*geom);
+  if (rc) return rc;
+  auto P = std::make_unique<at_plan>();
+  P->p.kind = AT_GEOM_CONE;
+  P->p.cone = *geom;
+  P->p.geom.n = geom->nx;
+  P->p.geom.pixel_mm = geom->voxel_mm;
+  P->p.geom.nviews = geom->nproj;
+  P->p.geom.ndets = geom->ndx * geom->ndy;
+  cudaStream_t st;
+  AT_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  rc = build_cone_plan(P->p, st);
+  cudaStreamSynchronize(st);
+  cudaStreamDestroy(st);
+  if (rc) return rc;
+  *out = P.release();
+  return AT_OK;
+}
+
 AT_API int at_plan_create_goldnc(at_plan **out) {
   AT_CHECK_ARG(out, "at_plan_create_goldnc: null argument");
   *out = nullptr;
@@ -193,6 +216,7 @@ AT_API int at_plan_get_stats(const at_plan *plan, at_plan_stats *out) {
   out->max_segments = p.max_segments;
   out->fp_rays_per_thread = p.fp_rpt;
   out->bp_runs = p.nruns;
+  out->nz = p.nz;
   return AT_OK;
 }
 
@@ -216,6 +240,7 @@ AT_API int at_plan_trace_ray(const at_plan *plan, int32_t view, int32_t det, int
     return AT_OK;
   }
   AT_CHECK_ARG(view >= 0 && view < p.nviews && det >= 0 && det < p.ndets, "at_plan_trace_ray: ray out of range");
+  if (p.kind == AT_GEOM_CONE) return cone_trace_ray(p, (int64_t)view * p.ndets + det, h_pix, h_w, cap, n_out);
   RayHdr h;
   AT_CUDA_TRY(cudaMemcpy(&h, p.rays_d + (size_t)view * p.ndets + det, sizeof(h), cudaMemcpyDeviceToHost));
   const int blk = view * p.nblocks_per_view + det / kRayBlock;
@@ -260,7 +285,7 @@ AT_API int at_back(const at_plan *plan, const float *d_sino, float *d_img, void 
 
 namespace {
 int project_host(const Plan &p, bool forward, const float *h_in, float *h_out) {
-  const size_t npix = (size_t)p.n * p.n, nbins = (size_t)p.nviews * p.ndets;
+  const size_t npix = (size_t)p.nz * p.n * p.n, nbins = (size_t)p.nviews * p.ndets;
   const size_t nin = forward ? npix : nbins, nout = forward ? nbins : npix;
   float *din = nullptr, *dout = nullptr;
   cudaStream_t st = nullptr;

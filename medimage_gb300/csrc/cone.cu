@@ -1,0 +1,408 @@
+// cone.cu -- 3D cone-beam projectors, traced on the fly.
+//
+// Each thread walks one ray with the reference's single-precision Siddon
+// (industry3d/src/tracing.cpp:123-307) from the end points of its cone()
+// (tracing.cpp:51-81).  Every operation is an explicitly rounded intrinsic
+// (__fadd_rn, __fmul_rn, ...) in the reference's order, so the visited voxels
+// and the FP32 weights are bit-identical to the reference's whatever the
+// compiler's contraction settings.  Nothing per ray is stored: at 512^3 with
+// 720 x 768 x 1024 rays a stored traversal would take hundreds of GB.
+//
+// Forward: thread per ray (detector columns fastest, so a warp's rays are
+// neighbours and share voxels in L1/L2), FP32 products summed per 32 segments
+// and the partial sums Kahan-folded, then the fused epilogue of the 2D
+// projectors.  Back: thread per ray, each term w*r scaled to an integer (one
+// FFMA, magic-number rounding) and added into a 64-bit integer accumulator per
+// voxel; integer sums do not depend on order, so the result is deterministic
+// without float atomics.  A per-voxel pass converts, runs the epilogue and
+// leaves the accumulator zero.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "epilogue.cuh"
+#include "solver.h"
+
+namespace at {
+
+// State of one ray's walk (tracing.cpp:131-265).
+struct ConeWalk {
+  float lam0, lx, ly, lz, len_x, len_y, len_z;
+  float stop;  // the smallest float >= lambda_max - 0.05 (see cone_start)
+  int vx, vy, vz, sx, sy, sz;
+  bool empty;
+};
+
+// tracing.cpp:51-81 (cone) with utility.cpp:82-98 (rotate_2d: d = R x summed
+// from zero, k-major); cos and sin per view come from the host's libm
+__device__ __forceinline__ void cone_endpoints(const ScanDev &S, int view, int row, int col, float &sx, float &sy,
+                                               float &sz, float &dx, float &dy, float &dz) {
+  const float2 cs = S.cone_trig[view];
+  const float c = cs.x, s = cs.y, ns = -cs.y;
+  const float X0 = 0.0f, X1 = -S.sod;  // source (0, -SOD, 0)
+  float srcX = __fadd_rn(__fadd_rn(0.0f, __fmul_rn(c, X0)), __fmul_rn(ns, X1));
+  float srcY = __fadd_rn(__fadd_rn(0.0f, __fmul_rn(s, X0)), __fmul_rn(c, X1));
+  float srcZ = 0.0f;
+  float dX = __double2float_rn(__dadd_rn((double)(col - S.half_cols), 0.5));
+  dX = __fmul_rn(dX, S.pitch);
+  const float dY = __fsub_rn(S.sdd, S.sod);
+  float dZ = __double2float_rn(__dsub_rn((double)(S.half_rows - row), 0.5));
+  dZ = __fmul_rn(dZ, S.pitch);
+  const float dstX = __fadd_rn(__fadd_rn(0.0f, __fmul_rn(c, dX)), __fmul_rn(ns, dY));
+  const float dstY = __fadd_rn(__fadd_rn(0.0f, __fmul_rn(s, dX)), __fmul_rn(c, dY));
+  srcX = __fdiv_rn(srcX, S.voxel);
+  srcZ = __fdiv_rn(srcZ, S.voxel);
+  srcY = __fdiv_rn(srcY, S.voxel);
+  const float dxv = __fdiv_rn(dstX, S.voxel), dyv = __fdiv_rn(dstY, S.voxel), dzv = __fdiv_rn(dZ, S.voxel);
+  const double hx = S.n / 2.0, hz = S.nz / 2.0;  // NX/2.0 = NY/2.0, NZ/2.0
+  sx = __double2float_rn(__dadd_rn((double)srcX, hx));
+  sy = __double2float_rn(__dadd_rn((double)srcY, hx));
+  sz = __double2float_rn(__dadd_rn((double)srcZ, hz));
+  dx = __double2float_rn(__dadd_rn((double)dxv, hx));
+  dy = __double2float_rn(__dadd_rn((double)dyv, hx));
+  dz = __double2float_rn(__dadd_rn((double)dzv, hz));
+}
+
+// LAMBDA_X/Y/Z of tracing.cpp:101-103: L*((float)i - s)/(d - s)
+__device__ __forceinline__ float lam_at(float i, float s, float d, float L) {
+  return __fdiv_rn(__fmul_rn(L, __fsub_rn(i, s)), __fsub_rn(d, s));
+}
+
+// tracing.cpp:131-265: entry plane, first voxel and first crossings
+__device__ __forceinline__ ConeWalk cone_start(int nx, int ny, int nz, float sx, float sy, float sz, float dx,
+                                               float dy, float dz) {
+  ConeWalk w;
+  int index = 0;
+  const float ray_x = __fsub_rn(dx, sx), ray_y = __fsub_rn(dy, sy), ray_z = __fsub_rn(dz, sz);
+  const float L =
+      __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(ray_x, ray_x), __fmul_rn(ray_y, ray_y)), __fmul_rn(ray_z, ray_z)));
+  float lambda_min = 0.0f, lambda_max = L;
+  w.sx = (ray_x > 0) ? 1 : -1;
+  w.sy = (ray_y > 0) ? 1 : -1;
+  w.sz = (ray_z > 0) ? 1 : -1;
+  const float ax = fabsf(ray_x), ay = fabsf(ray_y), az = fabsf(ray_z);
+  w.len_x = ((double)ax > 1.e-4) ? __fdiv_rn(L, ax) : 1.e6f;
+  w.len_y = ((double)ay > 1.e-4) ? __fdiv_rn(L, ay) : 1.e6f;
+  w.len_z = ((double)az > 1.e-4) ? __fdiv_rn(L, az) : 1.e6f;
+  float l0, lN, t;
+  l0 = lam_at(0.f, sx, dx, L);
+  lN = lam_at((float)nx, sx, dx, L);
+  t = (l0 < lN) ? l0 : lN;
+  lambda_min = (lambda_min > t) ? lambda_min : t;
+  if (lambda_min == t) index = 1;
+  t = (l0 > lN) ? l0 : lN;
+  lambda_max = (lambda_max < t) ? lambda_max : t;
+  l0 = lam_at(0.f, sy, dy, L);
+  lN = lam_at((float)ny, sy, dy, L);
+  t = (l0 < lN) ? l0 : lN;
+  lambda_min = (lambda_min > t) ? lambda_min : t;
+  if (lambda_min == t) index = 2;
+  t = (l0 > lN) ? l0 : lN;
+  lambda_max = (lambda_max < t) ? lambda_max : t;
+  l0 = lam_at(0.f, sz, dz, L);
+  lN = lam_at((float)nz, sz, dz, L);
+  t = (l0 < lN) ? l0 : lN;
+  lambda_min = (lambda_min > t) ? lambda_min : t;
+  if (lambda_min == t) index = 3;
+  t = (l0 > lN) ? l0 : lN;
+  lambda_max = (lambda_max < t) ? lambda_max : t;
+  w.empty = !(lambda_min < lambda_max);  // tracing.cpp:214 (also false for NaN, as there)
+  if (w.empty) return w;
+  const float lam = lambda_min;
+  auto first = [&](float s, float r) { return (int)__fadd_rn(s, __fdiv_rn(__fmul_rn(lam, r), L)); };
+  auto cross = [&](int v, int sg, float s, float d, float a) {
+    return ((double)a < 1.e-4) ? 1.e6f : lam_at(__fadd_rn((float)v, (float)(sg > 0)), s, d, L);
+  };
+  if (index == 1) {
+    w.vx = (w.sx == 1) ? 0 : nx - 1;
+    w.lx = __fadd_rn(lam, w.len_x);
+    w.vy = first(sy, ray_y);
+    w.ly = cross(w.vy, w.sy, sy, dy, ay);
+    w.vz = first(sz, ray_z);
+    w.lz = cross(w.vz, w.sz, sz, dz, az);
+  } else if (index == 2) {
+    w.vy = (w.sy == 1) ? 0 : ny - 1;
+    w.ly = __fadd_rn(lam, w.len_y);
+    w.vx = first(sx, ray_x);
+    w.lx = cross(w.vx, w.sx, sx, dx, ax);
+    w.vz = first(sz, ray_z);
+    w.lz = cross(w.vz, w.sz, sz, dz, az);
+  } else {
+    w.vz = (w.sz == 1) ? 0 : nz - 1;
+    w.lz = __fadd_rn(lam, w.len_z);
+    w.vx = first(sx, ray_x);
+    w.lx = cross(w.vx, w.sx, sx, dx, ax);
+    w.vy = first(sy, ray_y);
+    w.ly = cross(w.vy, w.sy, sy, dy, ay);
+  }
+  w.lam0 = lam;
+  // the loop test of tracing.cpp:267, (double)lambda0 < (double)lambda_max -
+  // 0.05, as one float compare: a float x is below a double D exactly when it
+  // is below D rounded up to a float
+  w.stop = __double2float_ru(__dsub_rn((double)lambda_max, 5.e-2));
+  return w;
+}
+
+// tracing.cpp:267-306: calls f(on_grid, voxel, weight) per segment.  Each
+// step crosses one plane of the (nx+1) + (ny+1) + (nz+1) inside the clipped
+// segment, so the walk ends within nx + ny + nz + 3 steps; the bound below is
+// only a guard.
+template <typename F>
+__device__ __forceinline__ void cone_walk(ConeWalk &w, int nx, int ny, int nz, F &&f) {
+  const int64_t sxs = (int64_t)w.sx * ny, szs = (int64_t)w.sz * nx * ny;
+  int64_t addr = (int64_t)w.vz * nx * ny + (int64_t)w.vx * ny + w.vy;
+  const int guard = nx + ny + nz + 16;
+  for (int it = 0; w.lam0 < w.stop && it < guard; it++) {
+    const bool on = (unsigned)w.vx < (unsigned)nx && (unsigned)w.vy < (unsigned)ny && (unsigned)w.vz < (unsigned)nz;
+    if (w.lx <= w.ly && w.lx <= w.lz) {
+      f(on, addr, __fsub_rn(w.lx, w.lam0));
+      w.lam0 = w.lx;
+      w.lx = __fadd_rn(w.lx, w.len_x);
+      w.vx += w.sx;
+      addr += sxs;
+    } else if (w.ly <= w.lz) {
+      f(on, addr, __fsub_rn(w.ly, w.lam0));
+      w.lam0 = w.ly;
+      w.ly = __fadd_rn(w.ly, w.len_y);
+      w.vy += w.sy;
+      addr += w.sy;
+    } else {
+      f(on, addr, __fsub_rn(w.lz, w.lam0));
+      w.lam0 = w.lz;
+      w.lz = __fadd_rn(w.lz, w.len_z);
+      w.vz += w.sz;
+      addr += szs;
+    }
+  }
+}
+
+__device__ __forceinline__ ConeWalk cone_ray(const ScanDev &S, int64_t ray) {
+  const int per_view = S.ndx * S.ndy;
+  const int view = (int)(ray / per_view), rem = (int)(ray % per_view);
+  float sx, sy, sz, dx, dy, dz;
+  cone_endpoints(S, view, rem / S.ndy, rem % S.ndy, sx, sy, sz, dx, dy, dz);
+  return cone_start(S.n, S.n, S.nz, sx, sy, sz, dx, dy, dz);
+}
+
+constexpr int kConeThreads = 128;
+
+// ---------------------------------------------------------------------------
+// forward
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kConeThreads) cone_fp_kernel(const Launch L) {
+  const int scan = L.scans ? find_scan(L.prefix, L.nscans, blockIdx.x) : 0;
+  const ScanDev &S = scan_of(L, scan);
+  if (!flow_active(S, L.flow)) return;
+  const int cta0 = L.scans ? __ldg(L.prefix + scan) : 0;
+  const int ncta = L.scans ? __ldg(L.prefix + scan + 1) - cta0 : gridDim.x;
+  const int local_cta = blockIdx.x - cta0;
+  const int64_t ray = (int64_t)local_cta * kConeThreads + threadIdx.x;
+  double s0 = 0.0;
+  if (ray < S.nbins) {
+    const float *__restrict__ vol = S.buf[L.in_buf];
+    ConeWalk w = cone_ray(S, ray);
+    float acc = 0.f, comp = 0.f, part = 0.f;
+    int k = 0;
+    if (!w.empty)
+      cone_walk(w, S.n, S.n, S.nz, [&](bool on, int64_t addr, float wt) {
+        float val = 0.f;
+        if (on) val = __ldg(vol + addr);  // off-grid voxels are never read
+        part = fmaf(wt, val, part);
+        if ((++k & 31) == 0) {
+          kahan_add(acc, comp, part);
+          part = 0.f;
+        }
+      });
+    kahan_add(acc, comp, part);
+    fp_epilogue(S, L, (int)ray, acc - comp, s0);
+  }
+  if (stage_reduces(L.stage)) {
+    double v[1] = {s0};
+    reduce_and_finalize<1>(S, L, v, local_cta, ncta);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// back
+// ---------------------------------------------------------------------------
+constexpr int kConeTermBits = 22;  // |term| < 2^22, so one FFMA rounds it
+
+// fixed-point exponent from the scan's largest |r| (the 64 partial maxima of
+// sino_absmax_kernel); every CTA of both passes computes the same value.  Must
+// be reached by the whole CTA.
+__device__ __forceinline__ int cone_bp_sexp(const ScanDev &S) {
+  static_assert(kBpMaxParts == 64, "two partial maxima per lane");
+  __shared__ int s_sexp;
+  if (threadIdx.x < 32) {
+    float m = fmaxf(S.bpmax[threadIdx.x], S.bpmax[threadIdx.x + 32]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    // a segment is at most sqrt(3) voxels long: |w r| < 2 m
+    int ex = 0;
+    frexpf(fmaxf(2.f * m, 1e-30f), &ex);
+    if (threadIdx.x == 0) s_sexp = min(kConeTermBits - ex, 120);
+  }
+  __syncthreads();
+  return s_sexp;
+}
+
+__global__ void __launch_bounds__(kConeThreads) cone_bp_kernel(const Launch L) {
+  const int scan = L.scans ? find_scan(L.prefix, L.nscans, blockIdx.x) : 0;
+  const ScanDev &S = scan_of(L, scan);
+  if (!flow_active(S, L.flow)) return;
+  const int cta0 = L.scans ? __ldg(L.prefix + scan) : 0;
+  const int local_cta = blockIdx.x - cta0;
+  const int64_t ray = (int64_t)local_cta * kConeThreads + threadIdx.x;
+  const int sexp = cone_bp_sexp(S);
+  if (ray >= S.nbins) return;
+  const float r = S.buf[L.in_buf][ray];
+  if (r == 0.f) return;
+  const float rs = r * ldexpf(1.f, sexp);
+  constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
+  constexpr int kMagicBits = 0x4B400000;
+  ConeWalk w = cone_ray(S, ray);
+  if (w.empty) return;
+  unsigned long long *acc = S.bp_acc;
+  cone_walk(w, S.n, S.n, S.nz, [&](bool on, int64_t addr, float wt) {
+    if (on) {
+      const long long term = (long long)(__float_as_int(fmaf(wt, rs, kMagic)) - kMagicBits);
+      atomicAdd(acc + addr, (unsigned long long)term);
+    }
+  });
+}
+
+// per voxel, over the pixel-pass CTAs (8 x 32 tiles of each slice)
+__global__ void __launch_bounds__(256) cone_bp_finish_kernel(const Launch L) {
+  const int scan = L.scans ? find_scan(L.prefix, L.nscans, blockIdx.x) : 0;
+  const ScanDev &S = scan_of(L, scan);
+  if (!flow_active(S, L.flow)) return;
+  const int cta0 = L.scans ? __ldg(L.prefix + scan) : 0;
+  const int ncta = L.scans ? __ldg(L.prefix + scan + 1) - cta0 : gridDim.x;
+  const int local_cta = blockIdx.x - cta0;
+  const int n = S.n, tiles_y = (n + 31) >> 5, tiles = ((n + 7) >> 3) * tiles_y;
+  const int z = local_cta / tiles, t = local_cta % tiles;
+  const int x = (t / tiles_y) * 8 + (threadIdx.x >> 5), y = (t % tiles_y) * 32 + (threadIdx.x & 31);
+  const int sexp = cone_bp_sexp(S);
+  double s0 = 0.0;
+  if (x < n && y < n && z < S.nz) {
+    const int64_t i = ((int64_t)z * n + x) * n + y;
+    const long long total = (long long)atomicExch(S.bp_acc + i, 0ull);
+    const float val = (float)((double)total * ldexp(1.0, -sexp));
+    bp_epilogue(S, L, z, x, y, val, s0);
+  }
+  if (stage_reduces(L.stage)) {
+    double v[1] = {s0};
+    reduce_and_finalize<1>(S, L, v, local_cta, ncta);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// plan support: segment count, one traced ray
+// ---------------------------------------------------------------------------
+__global__ void cone_count_kernel(const ScanDev S, unsigned long long *segs, unsigned long long *offgrid,
+                                  int *maxseg) {
+  const int64_t ray = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  unsigned long long cnt = 0, off = 0;
+  if (ray < S.nbins) {
+    ConeWalk w = cone_ray(S, ray);
+    if (!w.empty)
+      cone_walk(w, S.n, S.n, S.nz, [&](bool on, int64_t, float) {
+        cnt++;
+        off += on ? 0 : 1;
+      });
+  }
+  const unsigned mine = (unsigned)cnt;
+  for (int o = 16; o > 0; o >>= 1) {
+    cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    off += __shfl_xor_sync(0xffffffffu, off, o);
+  }
+  const unsigned mx = __reduce_max_sync(0xffffffffu, mine);
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(segs, cnt);
+    atomicAdd(offgrid, off);
+    atomicMax(maxseg, (int)mx);
+  }
+}
+
+__global__ void cone_trace_one_kernel(const ScanDev S, int64_t ray, int cap, int *pix, float *wgt, int *count) {
+  ConeWalk w = cone_ray(S, ray);
+  int k = 0;
+  if (!w.empty)
+    cone_walk(w, S.n, S.n, S.nz, [&](bool, int64_t addr, float wt) {
+      if (k < cap) {
+        pix[k] = (int)addr;
+        wgt[k] = wt;
+      }
+      k++;
+    });
+  *count = k;
+}
+
+int cone_ctas(const ScanDev &S) { return (int)(((int64_t)S.nbins + kConeThreads - 1) / kConeThreads); }
+
+cudaError_t launch_cone_fp(const Launch &L, int nctas, cudaStream_t st) {
+  cone_fp_kernel<<<nctas, kConeThreads, 0, st>>>(L);
+  return cudaGetLastError();
+}
+
+// the max |r| pass has run; tracing pass over `L` (ray CTAs), then the
+// finishing pass over `Lpix` (pixel-pass CTAs)
+cudaError_t launch_cone_bp(const Launch &L, int nctas, const Launch &Lpix, int pix_nctas, cudaStream_t st) {
+  cone_bp_kernel<<<nctas, kConeThreads, 0, st>>>(L);
+  cone_bp_finish_kernel<<<pix_nctas, 256, 0, st>>>(Lpix);
+  return cudaGetLastError();
+}
+
+int build_cone_plan(Plan &p, cudaStream_t st) {
+  const at_cone_geometry &g = p.cone;
+  p.n = g.nx;
+  p.nz = g.nz;
+  p.nviews = g.nproj;
+  p.ndets = g.ndx * g.ndy;
+  p.rays = (int64_t)p.nviews * p.ndets;
+  std::vector<float2> trig(g.nproj);
+  cone_trig(g, trig.data());
+  AT_CUDA_TRY(cudaMalloc(&p.cone_trig_d, sizeof(float2) * g.nproj));
+  p.device_bytes += sizeof(float2) * g.nproj;
+  AT_CUDA_TRY(cudaMemcpyAsync(p.cone_trig_d, trig.data(), sizeof(float2) * g.nproj, cudaMemcpyHostToDevice, st));
+  ScanDev S;
+  fill_scan_plan(S, p);
+  unsigned long long *cnt = nullptr;
+  AT_CUDA_TRY(cudaMalloc(&cnt, 3 * sizeof(unsigned long long)));
+  AT_CUDA_TRY(cudaMemsetAsync(cnt, 0, 3 * sizeof(unsigned long long), st));
+  cone_count_kernel<<<(unsigned)((p.rays + 255) / 256), 256, 0, st>>>(S, cnt, cnt + 1, (int *)(cnt + 2));
+  AT_CUDA_TRY(cudaGetLastError());
+  unsigned long long h[3];
+  AT_CUDA_TRY(cudaMemcpyAsync(h, cnt, sizeof(h), cudaMemcpyDeviceToHost, st));
+  AT_CUDA_TRY(cudaStreamSynchronize(st));
+  cudaFree(cnt);
+  p.segments = (int64_t)h[0];
+  p.offgrid = (int64_t)h[1];
+  p.max_segments = (int)(unsigned)(h[2] & 0xffffffffu);
+  return AT_OK;
+}
+
+int cone_trace_ray(const Plan &p, int64_t ray, int32_t *h_pix, float *h_w, int32_t cap, int32_t *n_out) {
+  ScanDev S;
+  fill_scan_plan(S, p);
+  const int dcap = std::max(cap, 1);
+  int *pix = nullptr, *cnt = nullptr;
+  float *wgt = nullptr;
+  AT_CUDA_TRY(cudaMalloc(&pix, sizeof(int) * dcap));
+  AT_CUDA_TRY(cudaMalloc(&wgt, sizeof(float) * dcap));
+  AT_CUDA_TRY(cudaMalloc(&cnt, sizeof(int)));
+  cone_trace_one_kernel<<<1, 1>>>(S, ray, dcap, pix, wgt, cnt);
+  AT_CUDA_TRY(cudaGetLastError());
+  int n = 0;
+  AT_CUDA_TRY(cudaMemcpy(&n, cnt, sizeof(int), cudaMemcpyDeviceToHost));
+  const int m = std::min(n, cap);
+  if (m > 0 && h_pix) AT_CUDA_TRY(cudaMemcpy(h_pix, pix, sizeof(int) * m, cudaMemcpyDeviceToHost));
+  if (m > 0 && h_w) AT_CUDA_TRY(cudaMemcpy(h_w, wgt, sizeof(float) * m, cudaMemcpyDeviceToHost));
+  cudaFree(pix);
+  cudaFree(wgt);
+  cudaFree(cnt);
+  *n_out = n;
+  return AT_OK;
+}
+
+}  // namespace at

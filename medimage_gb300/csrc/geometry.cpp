@@ -61,4 +61,32 @@ int validate_rays(int n, double pixel_mm, int nviews, int ndets, const double *h
   return AT_OK;
 }
 
+// industry3d/src/tracing.cpp:57 and utility.cpp:84: theta =
+// (float)alpha/NPROJ*2*PI with the product by PI in double, then the float
+// overloads of cos and sin (cosf, sinf)
+void cone_trig(const at_cone_geometry &g, float2 *trig) {
+  constexpr double kPi = 3.1415926535897932385;  // ct3d.h:8
+  for (int a = 0; a < g.nproj; a++) {
+    const float t = (float)a / (float)g.nproj * 2;
+    const float theta = (float)((double)t * kPi);
+    trig[a] = make_float2(std::cos(theta), std::sin(theta));
+  }
+}
+
+int validate_cone(const at_cone_geometry &g) {
+  if (g.nx != g.ny) return set_error(AT_EINVAL, "cone geometry: nx must equal ny");
+  if (g.nx < 8 || g.nx > 4096 || g.nz < 1 || g.nz > 4096)
+    return set_error(AT_EINVAL, "cone geometry: nx in [8, 4096], nz in [1, 4096]");
+  if ((int64_t)g.nx * g.ny * g.nz > 2147483647ll) return set_error(AT_EINVAL, "cone geometry: volume above 2^31 voxels");
+  if (g.nproj < 1 || g.ndx < 1 || g.ndy < 1) return set_error(AT_EINVAL, "cone geometry: need nproj, ndx, ndy >= 1");
+  if ((int64_t)g.nproj * g.ndx * g.ndy > 2147483647ll) return set_error(AT_EINVAL, "cone geometry: above 2^31 rays");
+  if (!(g.voxel_mm > 0) || !(g.pitch_mm > 0) || !std::isfinite(g.voxel_mm) || !std::isfinite(g.pitch_mm))
+    return set_error(AT_EINVAL, "cone geometry: need voxel_mm > 0 and pitch_mm > 0");
+  if (!(g.sod_mm > 0) || !(g.sdd_mm > g.sod_mm) || !std::isfinite(g.sdd_mm))
+    return set_error(AT_EINVAL, "cone geometry: need 0 < sod_mm < sdd_mm");
+  const double half_diag = 0.5 * g.voxel_mm * std::sqrt(2.0 * (double)g.nx * g.nx + (double)g.nz * g.nz);
+  if (!(g.sod_mm > half_diag)) return set_error(AT_EINVAL, "cone geometry: the source must lie outside the volume");
+  return AT_OK;
+}
+
 }  // namespace at

@@ -712,6 +712,7 @@ Plan::~Plan() {
   cudaFree(gc_pair_off_d);
   cudaFree(gc_ent_d);
   cudaFree(gc_pix_off_d);
+  cudaFree(cone_trig_d);
 }
 
 }  // namespace at

@@ -21,89 +21,11 @@
 #include <algorithm>
 #include <cstring>
 
+#include "epilogue.cuh"
 #include "solver.h"
 
 namespace at {
 
-// ---------------------------------------------------------------------------
-// epilogues
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ void fp_epilogue(const ScanDev &S, const Launch &L, int bin, float val, double &s0) {
-  switch (L.stage) {
-    case ST_FP0: {  // r = g - Af ; E_data
-      const float g = S.buf[B_G][bin];
-      S.buf[B_R][bin] = g - val;
-      const double dv = (double)val - (double)g;
-      s0 += dv * dv;
-      if (L.aux_buf >= 0) S.buf[L.aux_buf][bin] = val;
-      break;
-    }
-    case ST_FPQ:  // q = A p ; |q|^2
-      S.buf[B_Q][bin] = val;
-      s0 += (double)val * (double)val;
-      break;
-    case ST_FPA: {  // E_data ; r -= c1 q
-      const float g = S.buf[B_G][bin];
-      const double dv = (double)val - (double)g;
-      s0 += dv * dv;
-      const float c1 = (float)S.ctl->c1;
-      S.buf[B_R][bin] = S.buf[B_R][bin] - c1 * S.buf[B_Q][bin];
-      if (L.aux_buf >= 0) S.buf[L.aux_buf][bin] = val;
-      break;
-    }
-    case ST_FPD:  // <A d, q>
-      s0 += (double)val * (double)S.buf[B_Q][bin];
-      if (L.aux_buf >= 0) S.buf[L.aux_buf][bin] = val;
-      break;
-    default:
-      S.buf[L.out_buf][bin] = val;
-      break;
-  }
-}
-
-__device__ __forceinline__ bool stage_reduces(int stage) {
-  return stage == ST_FP0 || stage == ST_FPQ || stage == ST_FPA || stage == ST_FPD || stage == ST_BP0 ||
-         stage == ST_BPD;
-}
-
-// d = A^T r + alpha * div-stencil (main.c:112-125, 226-239) and the smoothness
-// energy over the interior (main.c:135-139, 203-208).
-__device__ __forceinline__ void bp_epilogue(const ScanDev &S, const Launch &L, int x, int y, float val, double &s0) {
-  const int n = S.n;
-  const int i = x * n + y;
-  if (L.stage != ST_BP0 && L.stage != ST_BPD) {
-    S.buf[L.out_buf][i] = val;
-    return;
-  }
-  const float *u = S.buf[L.aux_buf];  // the update the stencil acts on
-  const float *v = S.buf[B_V];
-  const Ctl *c = S.ctl;
-  const float alpha = (float)c->alpha;
-  const float eps2 = (float)(0.01 * c->eps * c->eps);
-  const float Pc = v[i];
-  const float Pu = x > 0 ? v[i - n] : 1.f;
-  const float Pl = y > 0 ? v[i - 1] : 1.f;
-  const float Tc = u[i];
-  const float Td = x + 1 < n ? u[i + n] : 0.f;
-  const float Tr = y + 1 < n ? u[i + 1] : 0.f;
-  const float Tu = x > 0 ? u[i - n] : 0.f;
-  const float Tl = y > 0 ? u[i - 1] : 0.f;
-  const float Pc2 = Pc * Pc;
-  const float st = Pc2 * (Td - Tc) + Pc2 * (Tr - Tc) - Pu * Pu * (Tc - Tu) - Pl * Pl * (Tc - Tl) +
-                   eps2 * (Td + Tr - 4.f * Tc + Tu + Tl);
-  S.buf[B_D][i] = val + alpha * st;
-  if (x >= 1 && x <= n - 2 && y >= 1 && y <= n - 2) {
-    const double a = (double)Tc - (double)Tu, b = (double)Tc - (double)Tl;
-    s0 += (double)alpha * ((double)Pc2 + (double)eps2) * (a * a + b * b);
-  }
-}
-
-__device__ __forceinline__ void kahan_add(float &sum, float &comp, float x) {
-  const float y = x - comp;
-  const float t = sum + y;
-  comp = (t - sum) - y;
-  sum = t;
-}
 
 // ---------------------------------------------------------------------------
 // fan-beam forward projection
@@ -419,7 +341,7 @@ __global__ void __launch_bounds__(256) fan_bp_kernel(const Launch L) {
   double s0 = 0.0;
   if (finish && mine) {
     const float val = (float)((double)total * ldexp(1.0, -sexp));
-    bp_epilogue(S, L, x, y, val, s0);
+    bp_epilogue(S, L, 0, x, y, val, s0);
   }
   if (stage_reduces(L.stage)) {
     double v[1] = {s0};
@@ -554,7 +476,7 @@ __global__ void __launch_bounds__(256) gc_bp_kernel(const Launch L) {
     kahan_add(acc, comp, part);
   }
   double s0 = 0.0;
-  bp_epilogue(S, L, x, y, acc - comp, s0);
+  bp_epilogue(S, L, 0, x, y, acc - comp, s0);
   if (stage_reduces(L.stage)) {
     double v[1] = {s0};
     reduce_and_finalize<1>(S, L, v, local_cta, ncta);
@@ -564,14 +486,20 @@ __global__ void __launch_bounds__(256) gc_bp_kernel(const Launch L) {
 // ---------------------------------------------------------------------------
 // launch helpers
 // ---------------------------------------------------------------------------
+int cone_ctas(const ScanDev &S);
+cudaError_t launch_cone_fp(const Launch &L, int nctas, cudaStream_t st);
+cudaError_t launch_cone_bp(const Launch &L, int nctas, const Launch &Lpix, int pix_nctas, cudaStream_t st);
+
 int fp_ctas(const ScanDev &S, int rpt) {
   if (S.kind == AT_GEOM_GOLDNC) return (kGcFpWarps + 3) / 4;
+  if (S.kind == AT_GEOM_CONE) return cone_ctas(S);
   const int warps = S.nviews * S.nbpv * (4 / rpt);
   return (warps + 3) / 4;
 }
 
 int bp_ctas(const ScanDev &S) {
   if (S.kind == AT_GEOM_GOLDNC) return (kGcN / 8) * (kGcN / 32);
+  if (S.kind == AT_GEOM_CONE) return cone_ctas(S);
   return S.ntiles_y * S.ntiles_y * std::max(1, S.bp_split);
 }
 
@@ -584,11 +512,13 @@ int bp_split_for(int tiles, int nvb) {
   return std::max(1, std::min({s, nvb, kBpMaxSplit}));
 }
 
-int pix_ctas(const ScanDev &S) { return ((S.n + 7) / 8) * ((S.n + 31) / 32); }
+int pix_ctas(const ScanDev &S) { return ((S.n + 7) / 8) * ((S.n + 31) / 32) * S.nz; }
 
 cudaError_t launch_fp(const Launch &L, int kind, int rpt, int nctas, cudaStream_t st) {
   if (kind == AT_GEOM_GOLDNC) {
     gc_fp_kernel<<<nctas, 128, 0, st>>>(L);
+  } else if (kind == AT_GEOM_CONE) {
+    return launch_cone_fp(L, nctas, st);
   } else if (rpt == 4) {
     fan_fp_kernel<4><<<nctas, 128, 0, st>>>(L);
   } else if (rpt == 2) {
@@ -599,9 +529,15 @@ cudaError_t launch_fp(const Launch &L, int kind, int rpt, int nctas, cudaStream_
   return cudaGetLastError();
 }
 
-cudaError_t launch_bp(const Launch &L, int kind, int nctas, cudaStream_t st) {
+// Lpix / pix_nctas: the same launch over pixel-pass CTAs, for kernels whose
+// epilogue runs per pixel in a second pass (cone beam)
+cudaError_t launch_bp(const Launch &L, int kind, int nctas, cudaStream_t st, const Launch *Lpix, int pix_nctas) {
   if (kind == AT_GEOM_GOLDNC) {
     gc_bp_kernel<<<nctas, 256, 0, st>>>(L);
+  } else if (kind == AT_GEOM_CONE) {
+    if (!Lpix) return cudaErrorInvalidValue;
+    sino_absmax_kernel<<<(L.scans ? L.nscans : 1) * kBpMaxParts, 256, 0, st>>>(L);
+    return launch_cone_bp(L, nctas, *Lpix, pix_nctas, st);
   } else {
     sino_absmax_kernel<<<(L.scans ? L.nscans : 1) * kBpMaxParts, 256, 0, st>>>(L);
     fan_bp_kernel<<<nctas, 256, 0, st>>>(L);
@@ -617,7 +553,7 @@ namespace at {
 // keeps the fastest (results are bitwise identical across the three).
 int autotune_fan(Plan &p, cudaStream_t st) {
   p.fp_rpt = 1;
-  if (p.kind == AT_GEOM_GOLDNC) return AT_OK;
+  if (p.kind == AT_GEOM_GOLDNC || p.kind == AT_GEOM_CONE) return AT_OK;
   float *img = nullptr, *sino = nullptr;
   const size_t npix = (size_t)p.n * p.n, nbins = (size_t)p.nviews * p.ndets;
   AT_CUDA_TRY(cudaMallocAsync(&img, npix * sizeof(float), st));

@@ -205,7 +205,7 @@ AT_API void at_server_destroy(at_server *s) { delete s; }
 AT_API int at_server_submit(at_server *srv, at_plan *plan, const float *h_sino, int32_t iter_alt, double arrival_s,
                             int64_t *id) {
   if (!srv || !plan || !h_sino || !id) return set_error(AT_EINVAL, "at_server_submit: null argument");
-  if (plan->p.kind == AT_GEOM_GOLDNC)
+  if (plan->p.kind == AT_GEOM_GOLDNC || plan->p.kind == AT_GEOM_CONE)
     return set_error(AT_EINVAL, "at_server_submit: fan-beam and ray-table plans only");
   if (iter_alt < 1) return set_error(AT_EINVAL, "at_server_submit: iter_alt must be >= 1");
   Server &S = srv->s;

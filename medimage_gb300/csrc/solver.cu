@@ -20,7 +20,7 @@ int fp_ctas(const ScanDev &S, int rpt);
 int bp_ctas(const ScanDev &S);
 int pix_ctas(const ScanDev &S);
 cudaError_t launch_fp(const Launch &L, int kind, int rpt, int nctas, cudaStream_t st);
-cudaError_t launch_bp(const Launch &L, int kind, int nctas, cudaStream_t st);
+cudaError_t launch_bp(const Launch &L, int kind, int nctas, cudaStream_t st, const Launch *Lpix, int pix_nctas);
 cudaError_t launch_pixel(int which, const Launch &L, int nctas, cudaStream_t st);
 cudaError_t launch_flags(const ScanDev *scans, int nscans, int mode, cudaStream_t st);
 
@@ -30,7 +30,8 @@ void fill_scan_plan(ScanDev &S, const Plan &p) {
   S.n = p.n;
   S.nviews = p.nviews;
   S.ndets = p.ndets;
-  S.npix = p.n * p.n;
+  S.nz = p.nz;
+  S.npix = p.nz * p.n * p.n;
   S.nbins = p.nviews * p.ndets;
   S.nbpv = p.nblocks_per_view;
   S.offgrid = p.offgrid ? 1 : 0;
@@ -48,6 +49,15 @@ void fill_scan_plan(ScanDev &S, const Plan &p) {
   S.gc_pair_off = p.gc_pair_off_d;
   S.gc_ent = p.gc_ent_d;
   S.gc_pix_off = p.gc_pix_off_d;
+  S.ndx = p.cone.ndx;
+  S.ndy = p.cone.ndy;
+  S.half_rows = p.cone.half_rows;
+  S.half_cols = p.cone.half_cols;
+  S.voxel = p.cone.voxel_mm;
+  S.pitch = p.cone.pitch_mm;
+  S.sod = p.cone.sod_mm;
+  S.sdd = p.cone.sdd_mm;
+  S.cone_trig = p.cone_trig_d;
 }
 
 namespace {
@@ -62,7 +72,7 @@ struct ScanLayout {
 
 ScanLayout layout_of(const Plan &p, int rpt) {
   ScanLayout L;
-  const size_t npix = (size_t)p.n * p.n, nbins = (size_t)p.nviews * p.ndets;
+  const size_t npix = (size_t)p.nz * p.n * p.n, nbins = (size_t)p.nviews * p.ndets;
   L.img_bytes = align_up(npix * sizeof(float));
   L.sino_bytes = align_up(nbins * sizeof(float));
   ScanDev tmp;
@@ -102,7 +112,7 @@ void carve_scan(ScanDev &S, const Plan &p, int rpt, char *cur) {
 
 size_t bp_scratch_bytes(const Plan &p) {
   if (p.kind == AT_GEOM_GOLDNC) return 0;
-  return align_up(sizeof(unsigned long long) * (size_t)p.n * p.n) + align_up(sizeof(int) * (size_t)p.ntiles) +
+  return align_up(sizeof(unsigned long long) * (size_t)p.nz * p.n * p.n) + align_up(sizeof(int) * (size_t)p.ntiles) +
          align_up(sizeof(float) * kBpMaxParts);
 }
 
@@ -110,7 +120,7 @@ void carve_bp_scratch(ScanDev &S, const Plan &p, char *cur) {
   S.bp_split = 1;
   if (p.kind == AT_GEOM_GOLDNC) return;
   S.bp_acc = (unsigned long long *)cur;
-  cur += align_up(sizeof(unsigned long long) * (size_t)p.n * p.n);
+  cur += align_up(sizeof(unsigned long long) * (size_t)p.nz * p.n * p.n);
   S.bp_cnt = (int *)cur;
   cur += align_up(sizeof(int) * (size_t)p.ntiles);
   S.bpmax = (float *)cur;
@@ -152,7 +162,7 @@ int Batch::set(const ScanDev *scans, int n, int kind_, int rpt_, cudaStream_t st
   nscans = n;
   // back-projection split from the tiles of the whole launch
   std::vector<ScanDev> sc(scans, scans + n);
-  if (kind != AT_GEOM_GOLDNC) {
+  if (kind == AT_GEOM_FAN || kind == AT_GEOM_RAYS) {
     int tiles = 0, nvb = 1 << 30;
     for (const auto &S : sc) {
       tiles += S.ntiles_y * S.ntiles_y;
@@ -228,8 +238,11 @@ int Batch::enqueue_image(cudaStream_t st) {
     L.out_buf = B_D;
     L.aux_buf = u;
     L.k = k;
-    AT_CUDA_TRY(launch_bp(L, kind, bp_total, st));
-    launches++;
+    Launch Lp = L;  // the per-pixel finishing pass of the cone-beam back projector
+    Lp.prefix = prefix_d + FAM_PIX * (nscans + 1);
+    AT_CUDA_TRY(launch_bp(L, kind, bp_total, st, &Lp, pix_total));
+    // max |r| pass + back projection (+ per-pixel finish for the cone beam)
+    launches += kind == AT_GEOM_GOLDNC ? 1 : kind == AT_GEOM_CONE ? 3 : 2;
     return AT_OK;
   };
   auto pix = [&](int which, int flow, int stage, int in, int out, int aux, int k, int flag) -> int {
@@ -315,9 +328,11 @@ size_t Solver::footprint(const std::vector<Plan *> &plans, int rpt) {
 int Solver::create(const std::vector<Plan *> &pl, const at_params &prm) {
   if (pl.empty()) return set_error(AT_EINVAL, "solver: no scans");
   const int kind = pl[0]->kind;
+  // one batch runs one set of kernels: GoldenC, fan beam and ray tables, or cone beam
+  auto family = [](int k) { return k == AT_GEOM_RAYS ? AT_GEOM_FAN : k; };
   for (auto *p : pl)
-    if ((p->kind == AT_GEOM_GOLDNC) != (kind == AT_GEOM_GOLDNC))
-      return set_error(AT_EINVAL, "solver: GoldenC plans cannot share a batch with fan-beam or ray-table plans");
+    if (family(p->kind) != family(kind))
+      return set_error(AT_EINVAL, "solver: a batch holds GoldenC, fan-beam/ray-table or cone-beam plans, not a mix");
   if (prm.iter_image < 2) return set_error(AT_EINVAL, "solver: iter_image must be >= 2 (the reference divides by iter_image/2)");
   if (prm.iter_edge < 1 || prm.iter_alt < 0) return set_error(AT_EINVAL, "solver: iteration counts must be positive");
   if (prm.mode != 0 && prm.mode != 1) return set_error(AT_EINVAL, "solver: mode must be 0 (exact) or 1 (linear)");

@@ -78,7 +78,12 @@ constexpr int kBpMaxSplit = 8;   // most CTAs one back-projection tile is split 
 
 struct ScanDev {
   int kind, n, nviews, ndets;
+  int nz;                          // image slices (1 for 2D); npix = nz * n * n
   int npix, nbins, nbpv, offgrid;  // offgrid: the plan traces segments off the grid
+  // cone beam (n = nx = ny; ndets = ndx * ndy)
+  int ndx, ndy, half_rows, half_cols;
+  float voxel, pitch, sod, sdd;
+  const float2 *cone_trig;  // per view: cos, sin
   // fan plan
   const RayHdr *rays;
   const uint32_t *bits;

@@ -11,7 +11,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libat_engine.so")
 
-AT_GEOM_GOLDNC, AT_GEOM_FAN, AT_GEOM_RAYS = 0, 1, 2
+AT_GEOM_GOLDNC, AT_GEOM_FAN, AT_GEOM_RAYS, AT_GEOM_CONE = 0, 1, 2, 3
 _fp = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
@@ -40,6 +40,12 @@ class _FanGeom(C.Structure):
     ]
 
 
+class _ConeGeom(C.Structure):
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("voxel_mm", C.c_float),
+                ("nproj", C.c_int32), ("ndx", C.c_int32), ("ndy", C.c_int32), ("pitch_mm", C.c_float),
+                ("sod_mm", C.c_float), ("sdd_mm", C.c_float), ("half_rows", C.c_int32), ("half_cols", C.c_int32)]
+
+
 class _Params(C.Structure):
     _fields_ = [
         ("alpha", C.c_double),
@@ -65,6 +71,7 @@ class _PlanStats(C.Structure):
         ("max_segments", C.c_int32),
         ("fp_rays_per_thread", C.c_int32),
         ("bp_runs", C.c_int64),
+        ("nz", C.c_int32),
     ]
 
 
@@ -103,6 +110,7 @@ SIGNATURES = {
     "at_device_info": ([C.c_char_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_size_t)], C.c_int),
     "at_plan_create_fan": ([C.POINTER(_FanGeom), C.POINTER(C.c_void_p)], C.c_int),
     "at_plan_create_goldnc": ([C.POINTER(C.c_void_p)], C.c_int),
+    "at_plan_create_cone": ([C.POINTER(_ConeGeom), C.POINTER(C.c_void_p)], C.c_int),
     "at_plan_create_rays": ([C.c_int32, C.c_double, C.c_int32, C.c_int32, _dp, C.POINTER(C.c_void_p)], C.c_int),
     "at_plan_destroy": ([C.c_void_p], None),
     "at_plan_get_stats": ([C.c_void_p, C.POINTER(_PlanStats)], C.c_int),
@@ -308,6 +316,10 @@ class ConeGeometry:
         if self.half_cols < 0:
             self.half_cols = self.ndy // 2
 
+    def c(self) -> _ConeGeom:
+        return _ConeGeom(self.nx, self.ny, self.nz, self.voxel_mm, self.nproj, self.ndx, self.ndy, self.pitch_mm,
+                         self.sod_mm, self.sdd_mm, self.half_rows, self.half_cols)
+
 
 @dataclass
 class Params:
@@ -335,7 +347,13 @@ class Plan:
         st = _PlanStats()
         _check("at_plan_get_stats", lib().at_plan_get_stats(self._h, C.byref(st)))
         self.stats = {k: getattr(st, k) for k, _ in _PlanStats._fields_}
-        self.n, self.nviews, self.ndets = st.n, st.nviews, st.ndets
+        self.n, self.nviews, self.ndets, self.nz = st.n, st.nviews, st.ndets, st.nz
+        if st.kind == AT_GEOM_CONE:
+            self.img_shape = (st.nz, st.n, st.n)
+            self.sino_shape = (geom.nproj, geom.ndx, geom.ndy)
+        else:
+            self.img_shape = (st.n, st.n)
+            self.sino_shape = (st.nviews, st.ndets)
 
     @classmethod
     def fan(cls, geom: FanGeometry) -> "Plan":
@@ -349,6 +367,13 @@ class Plan:
         h = C.c_void_p()
         _check("at_plan_create_rays", lib().at_plan_create_rays(geom.n, geom.pixel_mm, geom.nviews, geom.ndets,
                                                                 geom.endpoints, C.byref(h)))
+        return cls(h, geom)
+
+    @classmethod
+    def cone(cls, geom: ConeGeometry) -> "Plan":
+        h = C.c_void_p()
+        g = geom.c()
+        _check("at_plan_create_cone", lib().at_plan_create_cone(C.byref(g), C.byref(h)))
         return cls(h, geom)
 
     @classmethod
@@ -382,15 +407,15 @@ class Plan:
 
     def forward(self, img: np.ndarray) -> np.ndarray:
         img = np.ascontiguousarray(img, np.float32)
-        assert img.shape == (self.n, self.n)
-        out = np.zeros((self.nviews, self.ndets), np.float32)
+        assert img.shape == self.img_shape
+        out = np.zeros(self.sino_shape, np.float32)
         _check("at_forward_host", lib().at_forward_host(self._h, img, out))
         return out
 
     def back(self, sino: np.ndarray) -> np.ndarray:
         sino = np.ascontiguousarray(sino, np.float32)
-        assert sino.shape == (self.nviews, self.ndets)
-        out = np.zeros((self.n, self.n), np.float32)
+        assert sino.shape == self.sino_shape
+        out = np.zeros(self.img_shape, np.float32)
         _check("at_back_host", lib().at_back_host(self._h, sino, out))
         return out
 
@@ -442,7 +467,7 @@ class Solver:
     def set_sino(self, scan: int, sino: np.ndarray, stream: int = 0) -> None:
         p = self.plans[scan]
         sino = np.ascontiguousarray(sino, np.float32)
-        assert sino.shape == (p.nviews, p.ndets)
+        assert sino.shape == p.sino_shape
         self._keep = sino  # host buffer must live until the copy completes
         _check("at_solver_set_sino_host", lib().at_solver_set_sino_host(self._h, scan, sino, C.c_void_p(stream)))
         self.sync(stream)
@@ -475,8 +500,8 @@ class Solver:
 
     def get(self, scan: int, stream: int = 0):
         p = self.plans[scan]
-        f = np.zeros((p.n, p.n), np.float32)
-        v = np.zeros((p.n, p.n), np.float32)
+        f = np.zeros(p.img_shape, np.float32)
+        v = np.zeros(p.img_shape, np.float32)
         _check("at_solver_get_host", lib().at_solver_get_host(self._h, scan, f, v, C.c_void_p(stream)))
         return f, v
 
@@ -499,8 +524,8 @@ class Solver:
 def reconstruct(plan: Plan, params: Params, sino: np.ndarray):
     """One call through at_reconstruct_host: host sinogram in, (f, v) out."""
     sino = np.ascontiguousarray(sino, np.float32)
-    f = np.zeros((plan.n, plan.n), np.float32)
-    v = np.zeros((plan.n, plan.n), np.float32)
+    f = np.zeros(plan.img_shape, np.float32)
+    v = np.zeros(plan.img_shape, np.float32)
     prm = params.c()
     _check("at_reconstruct_host", lib().at_reconstruct_host(plan.handle, C.byref(prm), sino, f, v))
     return f, v
@@ -542,8 +567,8 @@ class Server:
 
     def result(self, rid: int):
         p = self._plans[rid]
-        f = np.zeros((p.n, p.n), np.float32)
-        v = np.zeros((p.n, p.n), np.float32)
+        f = np.zeros(p.img_shape, np.float32)
+        v = np.zeros(p.img_shape, np.float32)
         lat, wait = C.c_double(), C.c_double()
         _check("at_server_result", lib().at_server_result(self._h, rid, f, v, C.byref(lat), C.byref(wait)))
         return f, v, lat.value, wait.value

@@ -450,17 +450,26 @@ void or_fan_AT(const or_fan_geom *g, double *img, const double *sino, int nthrea
 /* ========================================================================
  * Projector dispatch for the solver
  * ======================================================================== */
-int or_proj_views(const or_projector *P) { return P->kind == OR_PROJ_FAN ? P->fan.nviews : OR_GC_VIEWS; }
-int or_proj_dets(const or_projector *P) { return P->kind == OR_PROJ_FAN ? P->fan.ndets : OR_GC_DETS; }
-int or_proj_n(const or_projector *P) { return P->kind == OR_PROJ_FAN ? P->fan.n : OR_GC_N; }
+int or_proj_views(const or_projector *P) {
+    return P->kind == OR_PROJ_FAN ? P->fan.nviews : P->kind == OR_PROJ_CONE ? P->cone.nproj : OR_GC_VIEWS;
+}
+int or_proj_dets(const or_projector *P) {
+    return P->kind == OR_PROJ_FAN ? P->fan.ndets : P->kind == OR_PROJ_CONE ? P->cone.ndx * P->cone.ndy : OR_GC_DETS;
+}
+int or_proj_n(const or_projector *P) {
+    return P->kind == OR_PROJ_FAN ? P->fan.n : P->kind == OR_PROJ_CONE ? P->cone.nx : OR_GC_N;
+}
+int or_proj_nz(const or_projector *P) { return P->kind == OR_PROJ_CONE ? P->cone.nz : 1; }
 
 void or_proj_A(const or_projector *P, double *sino, const double *img) {
-    if (P->kind == OR_PROJ_FAN) or_fan_A(&P->fan, sino, img, P->nthreads);
+    if (P->kind == OR_PROJ_CONE) or_cone_A(&P->cone, sino, img, P->nthreads);
+    else if (P->kind == OR_PROJ_FAN) or_fan_A(&P->fan, sino, img, P->nthreads);
     else or_gc_A(sino, img);
 }
 
 void or_proj_AT(const or_projector *P, double *img, const double *sino) {
-    if (P->kind == OR_PROJ_FAN) or_fan_AT(&P->fan, img, sino, P->nthreads);
+    if (P->kind == OR_PROJ_CONE) or_cone_AT(&P->cone, img, sino, P->nthreads);
+    else if (P->kind == OR_PROJ_FAN) or_fan_AT(&P->fan, img, sino, P->nthreads);
     else or_gc_AStar(img, sino);
 }
 
@@ -543,12 +552,67 @@ void or_medfilt2(int n, double *f) {
     free(pf);
 }
 
+/* ---- volumes (nz > 1 slices; the cone beam).  Not in the reference: GoldenC
+ * is 2D.  The same functional with the z neighbours added to every
+ * stencil: backward differences in z in the smoothness term and its energy
+ * (interior in z as well), central differences in z in the edge step, a
+ * six-neighbour Laplacian scaled by 1/6 (GoldenC's 4-neighbour one is scaled
+ * by 1/4), and GoldenC's 3x3 median within each slice. ---- */
+static inline double pad3(const double *a, int n, int nz, int k, int i, int j, double fill) {
+    if (k < 1 || k > nz || i < 1 || j < 1 || i > n || j > n) return fill;
+    return a[((size_t)(k - 1) * n + (i - 1)) * n + (j - 1)];
+}
+
+static void image_gradient_stencil3(int n, int nz, double *d, const double *u, const double *v, double alpha,
+                                    double epsilon) {
+    for (int k = 1; k <= nz; ++k)
+        for (int i = 1; i <= n; ++i)
+            for (int j = 1; j <= n; ++j) {
+                double Pc = pad3(v, n, nz, k, i, j, 1.0), Pu = pad3(v, n, nz, k, i - 1, j, 1.0),
+                       Pl = pad3(v, n, nz, k, i, j - 1, 1.0), Pf = pad3(v, n, nz, k - 1, i, j, 1.0);
+                double Tc = pad3(u, n, nz, k, i, j, 0.0), Td = pad3(u, n, nz, k, i + 1, j, 0.0),
+                       Tr = pad3(u, n, nz, k, i, j + 1, 0.0), Tb = pad3(u, n, nz, k + 1, i, j, 0.0),
+                       Tu = pad3(u, n, nz, k, i - 1, j, 0.0), Tl = pad3(u, n, nz, k, i, j - 1, 0.0),
+                       Tf = pad3(u, n, nz, k - 1, i, j, 0.0);
+                d[((size_t)(k - 1) * n + (i - 1)) * n + (j - 1)] +=
+                    alpha * (sq(Pc) * (Td - Tc) + sq(Pc) * (Tr - Tc) + sq(Pc) * (Tb - Tc) - sq(Pu) * (Tc - Tu) -
+                             sq(Pl) * (Tc - Tl) - sq(Pf) * (Tc - Tf) +
+                             0.01 * sq(epsilon) * (Td + Tr + Tb - 6 * Tc + Tu + Tl + Tf));
+            }
+}
+
+static double smooth_energy3(int n, int nz, double acc, const double *u, const double *v, double alpha,
+                             double epsilon) {
+    for (int k = 2; k <= nz - 1; ++k)
+        for (int i = 2; i <= n - 1; ++i)
+            for (int j = 2; j <= n - 1; ++j) {
+                double P = pad3(v, n, nz, k, i, j, 1.0);
+                double Tc = pad3(u, n, nz, k, i, j, 0.0), Tu = pad3(u, n, nz, k, i - 1, j, 0.0),
+                       Tl = pad3(u, n, nz, k, i, j - 1, 0.0), Tf = pad3(u, n, nz, k - 1, i, j, 0.0);
+                acc += alpha * (sq(P) + 0.01 * sq(epsilon)) * (sq(Tc - Tu) + sq(Tc - Tl) + sq(Tc - Tf));
+            }
+    return acc;
+}
+
+static double nv3(int n, int nz, const double *p, const double *v, double epsilon) {
+    double nV = 0;
+    for (int k = 1; k <= nz; ++k)
+        for (int i = 1; i <= n; ++i)
+            for (int j = 1; j <= n; ++j) {
+                double Pv = pad3(v, n, nz, k, i, j, 1.0);
+                double Tc = pad3(p, n, nz, k, i, j, 0.0), Tu = pad3(p, n, nz, k, i - 1, j, 0.0),
+                       Tl = pad3(p, n, nz, k, i, j - 1, 0.0), Tf = pad3(p, n, nz, k - 1, i, j, 0.0);
+                nV += (sq(Pv) + 0.01 * sq(epsilon)) * (sq(Tc - Tu) + sq(Tc - Tl) + sq(Tc - Tf));
+            }
+    return nV;
+}
+
 void or_image_step(const or_projector *P, double *out, const double *g, const double *f,
                    const double *v, double alpha, double epsilon, int iter_image, or_trace *tr,
                    int outer) {
-    const int n = or_proj_n(P);
+    const int n = or_proj_n(P), nz = or_proj_nz(P);
     const int nb = or_proj_views(P) * or_proj_dets(P);
-    const int np = n * n;
+    const int np = nz * n * n;
     double *update = malloc(sizeof(double) * np), *d = malloc(sizeof(double) * np);
     double *p = malloc(sizeof(double) * np), *temp = malloc(sizeof(double) * np);
     double *Af = malloc(sizeof(double) * nb), *r = malloc(sizeof(double) * nb);
@@ -559,15 +623,19 @@ void or_image_step(const or_projector *P, double *out, const double *g, const do
     or_proj_A(P, Af, update);               /* :101 */
     for (int i = 0; i < nb; i++) r[i] = g[i] - Af[i];
     or_proj_AT(P, d, r); /* :110 */
-    image_gradient_stencil(n, d, update, v, alpha, epsilon);
+    if (nz == 1) image_gradient_stencil(n, d, update, v, alpha, epsilon);
+    else image_gradient_stencil3(n, nz, d, update, v, alpha, epsilon);
     AT_f_old = 0; /* :126-139 */
     for (int i = 0; i < nb; i++) AT_f_old += sq(Af[i] - g[i]);
-    AT_f_old = smooth_energy(n, AT_f_old, update, v, alpha, epsilon);
+    AT_f_old = nz == 1 ? smooth_energy(n, AT_f_old, update, v, alpha, epsilon)
+                      : smooth_energy3(n, nz, AT_f_old, update, v, alpha, epsilon);
     memcpy(p, d, sizeof(double) * np); /* :141-143 */
 
     for (int k = 1; k <= iter_image; ++k) { /* :145 */
         or_proj_A(P, q, p);
         nV = 0; /* :152-158, over all pixels */
+        if (nz > 1) nV = nv3(n, nz, p, v, epsilon);
+        else
         for (int i = 1; i <= n; ++i)
             for (int j = 1; j <= n; ++j) {
                 double Pv = pad_at(v, n, i, j, 1.0);
@@ -588,7 +656,8 @@ void or_image_step(const or_projector *P, double *out, const double *g, const do
             double CP = fabs(c_1 * p[i]);
             if (maxCP < CP) maxCP = CP;
         }
-        if (k % ((int)(iter_image / 2 + 0.0001)) == 0) or_medfilt2(n, update); /* :180-182 */
+        if (k % ((int)(iter_image / 2 + 0.0001)) == 0) /* :180-182, each slice */
+            for (int z = 0; z < nz; z++) or_medfilt2(n, update + (size_t)z * n * n);
 
         double sc[6] = {AT_f_old, nV, pSkalard, normAp, c_1, 0.0};
         if (k == iter_image) { /* :184-187 */
@@ -602,7 +671,8 @@ void or_image_step(const or_projector *P, double *out, const double *g, const do
         or_proj_A(P, Af, update); /* :193-208 */
         AT_f_new = 0;
         for (int i = 0; i < nb; i++) AT_f_new += sq(Af[i] - g[i]);
-        AT_f_new = smooth_energy(n, AT_f_new, update, v, alpha, epsilon);
+        AT_f_new = nz == 1 ? smooth_energy(n, AT_f_new, update, v, alpha, epsilon)
+                           : smooth_energy3(n, nz, AT_f_new, update, v, alpha, epsilon);
         if (1.1 * AT_f_old < AT_f_new && 1 < k) { /* :209-215 */
             memcpy(update, temp, sizeof(double) * np);
             trace_push(tr, outer, 0, k, sc, 5, 3);
@@ -611,7 +681,8 @@ void or_image_step(const or_projector *P, double *out, const double *g, const do
         AT_f_old = AT_f_new;
         for (int i = 0; i < nb; i++) r[i] -= c_1 * q[i]; /* :217-219 */
         or_proj_AT(P, d, r);                             /* :225 */
-        image_gradient_stencil(n, d, update, v, alpha, epsilon);
+        if (nz == 1) image_gradient_stencil(n, d, update, v, alpha, epsilon);
+        else image_gradient_stencil3(n, nz, d, update, v, alpha, epsilon);
         or_proj_A(P, Ad, d); /* :240-245 */
         AdSkalarAp = 0;
         for (int i = 0; i < nb; i++) AdSkalarAp += Ad[i] * q[i];
@@ -681,14 +752,81 @@ void or_edge_step(int n, double *out, const double *f, const double *v, double a
     free(update); free(temp); free(d); free(nn);
 }
 
+void or_edge_step_vol(int n, int nz, double *out, const double *f, const double *v, double alpha, double beta,
+                      double epsilon, int iter_edge, or_trace *tr, int outer) {
+    if (nz == 1) {
+        or_edge_step(n, out, f, v, alpha, beta, epsilon, iter_edge, tr, outer);
+        return;
+    }
+    const size_t np = (size_t)nz * n * n;
+    double *update = malloc(sizeof(double) * np), *temp = malloc(sizeof(double) * np);
+    double *d = malloc(sizeof(double) * np), *nn = malloc(sizeof(double) * np);
+    double nNablaD, nD, c;
+    memcpy(update, v, sizeof(double) * np);
+    for (int k = 1; k <= iter_edge; ++k) {
+        memcpy(temp, update, sizeof(double) * np);
+        for (int z = 1; z <= nz; ++z)
+            for (int i = 1; i <= n; ++i)
+                for (int j = 1; j <= n; ++j) {
+                    double dx = 0.5 * (pad3(f, n, nz, z, i + 1, j, 0.0) - pad3(f, n, nz, z, i - 1, j, 0.0));
+                    double dy = 0.5 * (pad3(f, n, nz, z, i, j + 1, 0.0) - pad3(f, n, nz, z, i, j - 1, 0.0));
+                    double dz = 0.5 * (pad3(f, n, nz, z + 1, i, j, 0.0) - pad3(f, n, nz, z - 1, i, j, 0.0));
+                    double nij = sq(dx) + sq(dy) + sq(dz);
+                    double Tc = pad3(temp, n, nz, z, i, j, 1.0);
+                    double lap = (1.0 / 6.0) * (pad3(temp, n, nz, z, i + 1, j, 1.0) + pad3(temp, n, nz, z, i, j + 1, 1.0) +
+                                                pad3(temp, n, nz, z + 1, i, j, 1.0) - 6 * Tc +
+                                                pad3(temp, n, nz, z, i - 1, j, 1.0) + pad3(temp, n, nz, z, i, j - 1, 1.0) +
+                                                pad3(temp, n, nz, z - 1, i, j, 1.0));
+                    double gij = alpha * Tc * nij - beta * epsilon * lap + beta * (Tc - 1) / (4 * epsilon);
+                    size_t idx = ((size_t)(z - 1) * n + (i - 1)) * n + (j - 1);
+                    nn[idx] = nij;
+                    d[idx] = -gij;
+                }
+        nNablaD = 0;
+        for (int z = 1; z <= nz; ++z)
+            for (int i = 1; i <= n; ++i)
+                for (int j = 1; j <= n; ++j)
+                    nNablaD = nNablaD + sq(0.5 * (pad3(d, n, nz, z, i + 1, j, 0.0) - pad3(d, n, nz, z, i - 1, j, 0.0))) +
+                              sq(0.5 * (pad3(d, n, nz, z, i, j + 1, 0.0) - pad3(d, n, nz, z, i, j - 1, 0.0))) +
+                              sq(0.5 * (pad3(d, n, nz, z + 1, i, j, 0.0) - pad3(d, n, nz, z - 1, i, j, 0.0)));
+        nD = 0;
+        for (size_t i = 0; i < np; i++) nD += sq(d[i]);
+        double tmp = 0;
+        for (size_t i = 0; i < np; i++) tmp += nn[i] * sq(d[i]);
+        c = nD / (alpha * tmp + beta * epsilon * nNablaD + (beta / (4 * epsilon)) * nD);
+        double maxCD = 0;
+        for (size_t i = 0; i < np; i++) {
+            update[i] = temp[i] + c * d[i];
+            double CD = fabs(c * d[i]);
+            if (CD > maxCD) maxCD = CD;
+        }
+        for (size_t i = 0; i < np; i++) {
+            if (update[i] > 1) update[i] = 1;
+            if (update[i] < 0) update[i] = 0;
+        }
+        double sc[3] = {nD, c, maxCD};
+        if (k == iter_edge) {
+            trace_push(tr, outer, 1, k, sc, 3, 1);
+            break;
+        }
+        if (maxCD < 1e-5) {
+            trace_push(tr, outer, 1, k, sc, 3, 2);
+            break;
+        }
+        trace_push(tr, outer, 1, k, sc, 3, 0);
+    }
+    memcpy(out, update, sizeof(double) * np);
+    free(update); free(temp); free(d); free(nn);
+}
+
 void or_solve(const or_projector *P, const double *g, double *f, double *v, double alpha,
               double beta, double epsilon, int iter_alt, int iter_image, int iter_edge,
               or_trace *tr) {
-    const int n = or_proj_n(P), np = n * n;
+    const int n = or_proj_n(P), nz = or_proj_nz(P), np = nz * n * n;
     memset(f, 0, sizeof(double) * np); /* main.c:36-40 */
     for (int i = 0; i < np; i++) v[i] = 1.0;
     for (int it = 1; it <= iter_alt; ++it) { /* main.c:43-47 */
         or_image_step(P, f, g, f, v, alpha, epsilon, iter_image, tr, it);
-        or_edge_step(n, v, f, v, alpha, beta, epsilon, iter_edge, tr, it);
+        or_edge_step_vol(n, nz, v, f, v, alpha, beta, epsilon, iter_edge, tr, it);
     }
 }

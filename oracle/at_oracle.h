@@ -104,11 +104,12 @@ void or_cone_A(const or_cone_geom *g, double *sino, const double *vol, int nthre
 void or_cone_AT(const or_cone_geom *g, double *vol, const double *sino, int nthreads);
 
 /* ---------------- AT solver (GoldenC main.c restated for any projector) ---- */
-enum { OR_PROJ_GOLDENC = 0, OR_PROJ_FAN = 1 };
+enum { OR_PROJ_GOLDENC = 0, OR_PROJ_FAN = 1, OR_PROJ_CONE = 2 };
 typedef struct {
     int kind;
     or_fan_geom fan;      /* used when kind == OR_PROJ_FAN */
     int nthreads;
+    or_cone_geom cone;    /* used when kind == OR_PROJ_CONE (a volume, nz slices) */
 } or_projector;
 
 /* Per-iteration scalars the reference prints (main.c:251,330), recorded so
@@ -131,6 +132,9 @@ void or_image_step(const or_projector *P, double *out, const double *g, const do
                    const double *v, double alpha, double epsilon, int iter_image,
                    or_trace *tr, int outer);
 /* main.c:259-360 */
+/* the edge step on a volume of nz slices (nz == 1: or_edge_step) */
+void or_edge_step_vol(int n, int nz, double *out, const double *f, const double *v, double alpha, double beta,
+                      double epsilon, int iter_edge, or_trace *tr, int outer);
 void or_edge_step(int n, double *out, const double *f, const double *v, double alpha,
                   double beta, double epsilon, int iter_edge, or_trace *tr, int outer);
 /* main.c:366-390 */
@@ -144,6 +148,7 @@ void or_solve(const or_projector *P, const double *g, double *f, double *v, doub
 int or_proj_views(const or_projector *P);
 int or_proj_dets(const or_projector *P);
 int or_proj_n(const or_projector *P);
+int or_proj_nz(const or_projector *P); /* slices: 1 for images */
 void or_proj_A(const or_projector *P, double *sino, const double *img);
 void or_proj_AT(const or_projector *P, double *img, const double *sino);
 

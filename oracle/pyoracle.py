@@ -55,7 +55,7 @@ class ConeGeom(C.Structure):
 
 
 class Projector(C.Structure):
-    _fields_ = [("kind", C.c_int), ("fan", FanGeom), ("nthreads", C.c_int)]
+    _fields_ = [("kind", C.c_int), ("fan", FanGeom), ("nthreads", C.c_int), ("cone", ConeGeom)]
 
 
 class TraceRec(C.Structure):
@@ -121,6 +121,8 @@ def lib() -> C.CDLL:
         L.or_cone_count_segments.restype = C.c_int64
         L.or_cone_A.argtypes = [C.POINTER(ConeGeom), _dp, _dp, C.c_int]
         L.or_cone_AT.argtypes = [C.POINTER(ConeGeom), _dp, _dp, C.c_int]
+        L.or_edge_step_vol.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, C.c_double, C.c_double, C.c_double, C.c_int,
+                                       C.POINTER(Trace), C.c_int]
         L.or_proj_A.argtypes = [C.POINTER(Projector), _dp, _dp]
         L.or_proj_AT.argtypes = [C.POINTER(Projector), _dp, _dp]
         _lib = L
@@ -164,10 +166,22 @@ def fan_from_engine(geom) -> Fan:
                geom.det_pitch_deg, geom.off_center, geom.view0_deg, geom.view_step_deg)
 
 
-def projector(fan: Fan | None, nthreads: int = 0) -> Projector:
-    if fan is None:
+def projector(geom, nthreads: int = 0) -> Projector:
+    """GoldenC (None), fan beam / ray table (Fan) or cone beam (an object
+    with the cone-geometry fields, e.g. ConeGeometry)."""
+    if geom is None:
         return Projector(0, FanGeom(), nthreads)
-    return Projector(1, fan.c(), nthreads)
+    if hasattr(geom, "ndx"):
+        return Projector(2, FanGeom(), nthreads, cone_c(geom))
+    return Projector(1, geom.c(), nthreads)
+
+
+def _image_shape(geom):
+    if geom is None:
+        return (GC_N, GC_N)
+    if hasattr(geom, "ndx"):
+        return (geom.nz, geom.nx, geom.ny)
+    return (geom.n, geom.n)
 
 
 # --------------------------------------------------------------------------
@@ -250,9 +264,8 @@ def solve(fan: Fan | None, g: np.ndarray, alpha: float, beta: float, epsilon: fl
     """FP64 AT reconstruction (GoldenC main.c:35-49) with the GoldenC projector
     (fan=None) or the fan-beam projector.  Returns (f, v, trace)."""
     P = projector(fan, nthreads)
-    n = GC_N if fan is None else fan.n
-    f = np.zeros((n, n), np.float64)
-    v = np.ones((n, n), np.float64)
+    f = np.zeros(_image_shape(fan), np.float64)
+    v = np.ones(_image_shape(fan), np.float64)
     tr, recs = _new_trace()
     lib().or_solve(C.byref(P), np.ascontiguousarray(g, np.float64), f, v, alpha, beta, epsilon,
                    iter_alt, iter_image, iter_edge, C.byref(tr))
@@ -270,11 +283,13 @@ def image_step(fan: Fan | None, g, f, v, alpha, epsilon, iter_image, nthreads: i
 
 
 def edge_step(f, v, alpha, beta, epsilon, iter_edge):
-    n = f.shape[0]
-    out = np.zeros((n, n), np.float64)
+    """GoldenC's edge step on an image (n, n) or a volume (nz, n, n)."""
+    f = np.ascontiguousarray(f, np.float64)
+    nz, n = (1, f.shape[0]) if f.ndim == 2 else (f.shape[0], f.shape[1])
+    out = np.zeros(f.shape, np.float64)
     tr, recs = _new_trace()
-    lib().or_edge_step(n, out, np.ascontiguousarray(f, np.float64), np.ascontiguousarray(v, np.float64),
-                       alpha, beta, epsilon, iter_edge, C.byref(tr), 1)
+    lib().or_edge_step_vol(n, nz, out, f, np.ascontiguousarray(v, np.float64), alpha, beta, epsilon, iter_edge,
+                           C.byref(tr), 1)
     return out, _trace_list(tr, recs)
 
 

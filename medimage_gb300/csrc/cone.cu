@@ -154,25 +154,23 @@ __device__ __forceinline__ void cone_walk(ConeWalk &w, int nx, int ny, int nz, F
   const int guard = nx + ny + nz + 16;
   for (int it = 0; w.lam0 < w.stop && it < guard; it++) {
     const bool on = (unsigned)w.vx < (unsigned)nx && (unsigned)w.vy < (unsigned)ny && (unsigned)w.vz < (unsigned)nz;
-    if (w.lx <= w.ly && w.lx <= w.lz) {
-      f(on, addr, __fsub_rn(w.lx, w.lam0));
-      w.lam0 = w.lx;
-      w.lx = __fadd_rn(w.lx, w.len_x);
-      w.vx += w.sx;
-      addr += sxs;
-    } else if (w.ly <= w.lz) {
-      f(on, addr, __fsub_rn(w.ly, w.lam0));
-      w.lam0 = w.ly;
-      w.ly = __fadd_rn(w.ly, w.len_y);
-      w.vy += w.sy;
-      addr += w.sy;
-    } else {
-      f(on, addr, __fsub_rn(w.lz, w.lam0));
-      w.lam0 = w.lz;
-      w.lz = __fadd_rn(w.lz, w.len_z);
-      w.vz += w.sz;
-      addr += szs;
-    }
+    // the reference's three-way test (x if lx is the smallest or tied, else y
+    // if ly <= lz, else z) as selects: neighbouring rays step differently, so
+    // branches would run every path for the whole warp
+    const bool bx = (w.lx <= w.ly) & (w.lx <= w.lz);
+    const bool by = !bx & (w.ly <= w.lz);
+    const bool bz = !bx & !by;
+    const float cur = bx ? w.lx : (by ? w.ly : w.lz);
+    f(on, addr, __fsub_rn(cur, w.lam0));
+    w.lam0 = cur;
+    const float nlx = __fadd_rn(w.lx, w.len_x), nly = __fadd_rn(w.ly, w.len_y), nlz = __fadd_rn(w.lz, w.len_z);
+    w.lx = bx ? nlx : w.lx;
+    w.ly = by ? nly : w.ly;
+    w.lz = bz ? nlz : w.lz;
+    w.vx += bx ? w.sx : 0;
+    w.vy += by ? w.sy : 0;
+    w.vz += bz ? w.sz : 0;
+    addr += bx ? sxs : (by ? (int64_t)w.sy : szs);
   }
 }
 

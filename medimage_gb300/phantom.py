@@ -109,3 +109,42 @@ def msbeam_phantom() -> np.ndarray:
             c0, c1 = (238, 256) if p % 2 == 0 else (256, 274)
             f[r0 + 2 * p:r0 + 2 * p + 2, c0:c1] = 2.0
     return f
+
+
+def csg_phantom(n: int, nz: int, seed: int = 0, n_parts: int | None = None, n_voids: int = 50,
+                mu: float = 0.02) -> np.ndarray:
+    """Seeded industrial-CT volume (nz, n, n): a part built from 8-16 solid
+    ellipsoids and z-axis cylinders (attenuation mu..1.5 mu per voxel) inside
+    the inscribed cylinder, with `n_voids` small spherical voids.  Each
+    primitive is evaluated inside its bounding box only."""
+    rng = np.random.default_rng(np.random.PCG64(seed))
+    vol = np.zeros((nz, n, n), np.float32)
+    parts = int(rng.integers(8, 17)) if n_parts is None else n_parts
+    c, cz = (n - 1) / 2.0, (nz - 1) / 2.0
+
+    def box(center, radii):
+        lo = [max(0, int(np.floor(center[k] - radii[k]))) for k in range(3)]
+        hi = [min(s, int(np.ceil(center[k] + radii[k])) + 1) for k, s in enumerate((nz, n, n))]
+        z, x, y = np.ogrid[lo[0]:hi[0], lo[1]:hi[1], lo[2]:hi[2]]
+        return (slice(lo[0], hi[0]), slice(lo[1], hi[1]), slice(lo[2], hi[2])), z, x, y
+
+    for _ in range(parts):
+        rz = rng.uniform(0.1, 0.35) * nz
+        rx, ry = rng.uniform(0.06, 0.22, 2) * n
+        cen = (cz + rng.uniform(-0.2, 0.2) * nz, c + rng.uniform(-0.2, 0.2) * n, c + rng.uniform(-0.2, 0.2) * n)
+        val = np.float32(mu * rng.uniform(1.0, 1.5))
+        sl, z, x, y = box(cen, (rz, rx, ry))
+        if rng.uniform() < 0.5:  # ellipsoid
+            m = ((z - cen[0]) / rz) ** 2 + ((x - cen[1]) / rx) ** 2 + ((y - cen[2]) / ry) ** 2 <= 1.0
+        else:  # cylinder along z
+            m = (((x - cen[1]) / rx) ** 2 + ((y - cen[2]) / ry) ** 2 <= 1.0) & (np.abs(z - cen[0]) <= rz)
+        sub = vol[sl]
+        sub[np.broadcast_to(m, sub.shape)] = val
+    for _ in range(n_voids):
+        r = rng.uniform(0.005, 0.02) * n
+        cen = (cz + rng.uniform(-0.3, 0.3) * nz, c + rng.uniform(-0.25, 0.25) * n, c + rng.uniform(-0.25, 0.25) * n)
+        sl, z, x, y = box(cen, (r, r, r))
+        m = (z - cen[0]) ** 2 + (x - cen[1]) ** 2 + (y - cen[2]) ** 2 <= r * r
+        sub = vol[sl]
+        sub[np.broadcast_to(m, sub.shape)] = 0.0
+    return vol

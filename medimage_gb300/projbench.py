@@ -1,11 +1,12 @@
 """Time the forward and back projectors alone on one workload geometry.
 
-    python -m medimage_gb300.projbench [--config c1|c2] [--reps N] [--which fp,bp]
+    python -m medimage_gb300.projbench [--config c1|c2|c4] [--n N] [--reps N] [--which fp,bp]
 
 Prints one JSON line per projector: average launch time (CUDA events on the
 launching stream), algorithmic bytes per launch (forward 4 S + 4 R, back
-4 S + 4 P; S segments, R rays, P pixels) and the resulting GB/s.  Used as the
-command under the profiler as well.
+4 S + 4 P; S segments, R rays, P pixels or voxels) and the resulting GB/s.
+Used as the command under the profiler as well.  c4 is the 512^3 cone beam
+(--n shrinks the volume, same field of view).
 """
 from __future__ import annotations
 
@@ -20,18 +21,25 @@ from . import configs, engine, phantom
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--config", default="c2", choices=["c1", "c2"])
+    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c4"])
+    ap.add_argument("--n", type=int, default=512, help="c4 volume edge (voxels)")
     ap.add_argument("--reps", type=int, default=20)
     ap.add_argument("--which", default="fp,bp")
     args = ap.parse_args()
-    spec = getattr(configs, args.config)()
-    plan = engine.Plan.fan(spec.geom)
+    if args.config == "c4":
+        spec = configs.c4(n=args.n, nz=args.n)
+        plan = engine.Plan.cone(spec.geom)
+        img = phantom.csg_phantom(args.n, args.n, seed=spec.seed)
+        names = ("cone_fp_kernel", "cone_bp_kernel")
+    else:
+        spec = getattr(configs, args.config)()
+        plan = engine.Plan.fan(spec.geom)
+        img = phantom.ellipse_phantom(plan.n, seed=spec.seed, n_random=spec.n_random)
+        names = ("fan_fp_kernel", "fan_bp_kernel")
     L = engine.lib()
     st = C.c_void_p()
     engine._check("at_stream_create", L.at_stream_create(C.byref(st)))
-    n, nv, nd = plan.n, plan.nviews, plan.ndets
-    img = phantom.ellipse_phantom(n, seed=spec.seed, n_random=spec.n_random)
-    sino = np.random.default_rng(0).standard_normal((nv, nd)).astype(np.float32)
+    sino = np.random.default_rng(0).standard_normal(plan.sino_shape).astype(np.float32)
     bufs = {}
     for name, arr in (("img", img), ("sino", sino), ("img_out", img), ("sino_out", sino)):
         p = C.c_void_p()
@@ -41,10 +49,10 @@ def main() -> None:
     import torch
 
     ts = torch.cuda.ExternalStream(st.value)
-    S, R, P = plan.stats["segments"], plan.stats["rays"], n * n
+    S, R, P = plan.stats["segments"], plan.stats["rays"], int(np.prod(plan.img_shape))
     jobs = {
-        "fp": ("fan_fp_kernel", lambda: plan.forward_dev(bufs["img"], bufs["sino_out"], st.value), 4 * S + 4 * R),
-        "bp": ("fan_bp_kernel", lambda: plan.back_dev(bufs["sino"], bufs["img_out"], st.value), 4 * S + 4 * P),
+        "fp": (names[0], lambda: plan.forward_dev(bufs["img"], bufs["sino_out"], st.value), 4 * S + 4 * R),
+        "bp": (names[1], lambda: plan.back_dev(bufs["sino"], bufs["img_out"], st.value), 4 * S + 4 * P),
     }
     for key in args.which.split(","):
         kname, fn, nbytes = jobs[key]
@@ -57,7 +65,8 @@ def main() -> None:
         e1.record(ts)
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / args.reps
-        print(json.dumps({"kernel": kname, "config": args.config, "launch_ms": round(ms, 5),
+        print(json.dumps({"kernel": kname, "config": args.config, "shape": list(plan.img_shape),
+                          "launch_ms": round(ms, 5), "gsegs_per_s": round(S / (ms / 1e3) / 1e9, 2),
                           "algorithmic_bytes": nbytes, "gbs": round(nbytes / (ms / 1e3) / 1e9, 1),
                           "segments": S, "rays": R, "pixels": P}))
     for p in bufs.values():

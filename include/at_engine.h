@@ -200,6 +200,37 @@ int at_psnr(const float *d_x, const float *d_ref, int64_t n, double peak, double
 int at_ssim(const float *d_x, const float *d_ref, int32_t h, int32_t w, double dynamic_range, double *h_ssim,
             void *stream);
 
+/* ---- row-action AT: msbeam/CPU_OpenMP on the GPU ----
+ * msbeam's algorithm (msbeam/CPU_OpenMP/src/main.c:213-394): per ray, one
+ * gradient step of the image (minIMAGE) and one of the edge field (minEDGE) on
+ * the ray's pixels, sweeping all rays of its parallel beam (proj.c:53-211:
+ * view k at pi*k/nproj, ray r at offset r - nray/2 pixels) with a step that
+ * shrinks after each sweep.  The reference races over views with OpenMP; here
+ * the rays of a view that are `phases` apart run together (they share no
+ * pixel or neighbour) and views and phases follow one another, so the result
+ * is deterministic.  Images n x n, sinograms [nproj][nray], nslices of each
+ * side by side. */
+typedef struct at_rowaction at_rowaction;
+typedef struct at_rowaction_params {
+    float alpha;        /* ALPHA (proto.h:8; 10)                                   */
+    double beta;        /* BETA (0.35)                                             */
+    double epsilon;     /* EPSILON (0.001)                                         */
+    float lambda0;      /* first step (main.c:371; 0.001)                          */
+    float lambda_decay; /* after a sweep lambda <- lambda/(1 + decay*lambda) (500) */
+    int32_t sweeps;     /* ALL_ITER (10)                                           */
+    int32_t phases;     /* >= 3; 4 by default                                      */
+} at_rowaction_params;
+/* traces msbeam's rays once (wray, bit-identical) and keeps them on the device */
+int at_rowaction_create(int32_t n, int32_t nproj, int32_t nray, at_rowaction **out);
+void at_rowaction_destroy(at_rowaction *ra);
+int at_rowaction_segments(const at_rowaction *ra, int64_t *segments);
+/* pixels (index y*n + x as msbeam addresses them) and weights of one ray */
+int at_rowaction_trace(const at_rowaction *ra, int32_t view, int32_t ray, int32_t *h_pix, float *h_w, int32_t cap,
+                       int32_t *n_out);
+/* f = 0, v = 1, then the sweeps (main.c:364-394); device buffers on `stream` */
+int at_rowaction_run(const at_rowaction *ra, int32_t nslices, const float *d_g, float *d_f, float *d_v,
+                     const at_rowaction_params *prm, void *stream);
+
 /* ---- continuous-batching server ----
  * Requests are admitted into a running batch once they have arrived and
  * their device state fits the HBM budget and a slot is free; every round

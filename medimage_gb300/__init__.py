@@ -14,6 +14,8 @@ from .engine import (  # noqa: F401
     ConeGeometry,
     FanGeometry,
     RayGeometry,
+    RowAction,
+    RowActionParams,
     Params,
     Plan,
     Server,
@@ -30,6 +32,8 @@ __all__ = [
     "ConeGeometry",
     "FanGeometry",
     "RayGeometry",
+    "RowAction",
+    "RowActionParams",
     "Params",
     "Plan",
     "Server",

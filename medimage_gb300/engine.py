@@ -46,6 +46,11 @@ class _ConeGeom(C.Structure):
                 ("sod_mm", C.c_float), ("sdd_mm", C.c_float), ("half_rows", C.c_int32), ("half_cols", C.c_int32)]
 
 
+class _RowActionParams(C.Structure):
+    _fields_ = [("alpha", C.c_float), ("beta", C.c_double), ("epsilon", C.c_double), ("lambda0", C.c_float),
+                ("lambda_decay", C.c_float), ("sweeps", C.c_int32), ("phases", C.c_int32)]
+
+
 class _Params(C.Structure):
     _fields_ = [
         ("alpha", C.c_double),
@@ -110,6 +115,12 @@ SIGNATURES = {
     "at_device_info": ([C.c_char_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_size_t)], C.c_int),
     "at_plan_create_fan": ([C.POINTER(_FanGeom), C.POINTER(C.c_void_p)], C.c_int),
     "at_plan_create_goldnc": ([C.POINTER(C.c_void_p)], C.c_int),
+    "at_rowaction_create": ([C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)], C.c_int),
+    "at_rowaction_destroy": ([C.c_void_p], None),
+    "at_rowaction_segments": ([C.c_void_p, C.POINTER(C.c_int64)], C.c_int),
+    "at_rowaction_trace": ([C.c_void_p, C.c_int32, C.c_int32, _ip, _fp, C.c_int32, C.POINTER(C.c_int32)], C.c_int),
+    "at_rowaction_run": ([C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(_RowActionParams),
+                          C.c_void_p], C.c_int),
     "at_plan_create_cone": ([C.POINTER(_ConeGeom), C.POINTER(C.c_void_p)], C.c_int),
     "at_plan_create_rays": ([C.c_int32, C.c_double, C.c_int32, C.c_int32, _dp, C.POINTER(C.c_void_p)], C.c_int),
     "at_plan_destroy": ([C.c_void_p], None),
@@ -577,6 +588,88 @@ class Server:
         st = _ServerStats()
         _check("at_server_get_stats", lib().at_server_get_stats(self._h, C.byref(st)))
         return {k: getattr(st, k) for k, _ in _ServerStats._fields_}
+
+
+@dataclass
+class RowActionParams:
+    """msbeam/CPU_OpenMP's constants (proto.h:8-12, main.c:371,391)."""
+
+    alpha: float = 10.0
+    beta: float = 0.35
+    epsilon: float = 0.001
+    lambda0: float = 0.001
+    lambda_decay: float = 500.0
+    sweeps: int = 10
+    phases: int = 4
+
+    def c(self) -> _RowActionParams:
+        return _RowActionParams(self.alpha, self.beta, self.epsilon, self.lambda0, self.lambda_decay, self.sweeps,
+                                self.phases)
+
+
+class RowAction:
+    """msbeam's row-action AT on the GPU (at_rowaction_*): its parallel beam of
+    nproj views x nray rays over an n x n image (defaults: msbeam's 512, 180,
+    768)."""
+
+    def __init__(self, n: int = 512, nproj: int = 180, nray: int = 768):
+        self.n, self.nproj, self.nray = n, nproj, nray
+        self._h = C.c_void_p()
+        _check("at_rowaction_create", lib().at_rowaction_create(n, nproj, nray, C.byref(self._h)))
+        seg = C.c_int64()
+        _check("at_rowaction_segments", lib().at_rowaction_segments(self._h, C.byref(seg)))
+        self.segments = seg.value
+
+    def close(self):
+        if self._h:
+            lib().at_rowaction_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def trace(self, view: int, ray: int):
+        cap = 4 * self.n
+        pix = np.zeros(cap, np.int32)
+        w = np.zeros(cap, np.float32)
+        k = C.c_int32()
+        _check("at_rowaction_trace", lib().at_rowaction_trace(self._h, view, ray, pix, w, cap, C.byref(k)))
+        return pix[: k.value].copy(), w[: k.value].copy()
+
+    def run_dev(self, nslices: int, d_g: int, d_f: int, d_v: int, params: RowActionParams | None = None,
+                stream: int = 0) -> None:
+        prm = (params or RowActionParams()).c()
+        _check("at_rowaction_run", lib().at_rowaction_run(self._h, nslices, C.c_void_p(d_g), C.c_void_p(d_f),
+                                                          C.c_void_p(d_v), C.byref(prm), C.c_void_p(stream)))
+
+    def run(self, g: np.ndarray, params: RowActionParams | None = None):
+        """g: [nproj][nray] or [slices][nproj][nray] host sinograms; returns
+        (f, v) with matching leading shape."""
+        g = np.ascontiguousarray(g, np.float32)
+        single = g.ndim == 2
+        gs = g.reshape(-1, self.nproj, self.nray)
+        B = gs.shape[0]
+        L = lib()
+        ptr = []
+        try:
+            for nbytes in (gs.nbytes, B * self.n * self.n * 4, B * self.n * self.n * 4):
+                p = C.c_void_p()
+                _check("at_dev_alloc", L.at_dev_alloc(C.byref(p), nbytes))
+                ptr.append(p.value)
+            _check("h2d", L.at_memcpy_h2d(C.c_void_p(ptr[0]), gs.ctypes.data, gs.nbytes, None))
+            self.run_dev(B, ptr[0], ptr[1], ptr[2], params)
+            f = np.zeros((B, self.n, self.n), np.float32)
+            v = np.zeros((B, self.n, self.n), np.float32)
+            _check("d2h", L.at_memcpy_d2h(f.ctypes.data, C.c_void_p(ptr[1]), f.nbytes, None))
+            _check("d2h", L.at_memcpy_d2h(v.ctypes.data, C.c_void_p(ptr[2]), v.nbytes, None))
+            _check("sync", L.at_stream_sync(None))
+        finally:
+            for p in ptr:
+                L.at_dev_free(C.c_void_p(p))
+        return (f[0], v[0]) if single else (f, v)
 
 
 def quality(x: np.ndarray, ref: np.ndarray, peak: float = 0.0, dynamic_range: float | None = None) -> dict:

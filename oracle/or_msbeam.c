@@ -249,6 +249,29 @@ void or_ms_solve(const float *g, float *f, float *v, int iters, int nthreads) {
     }
 }
 
+/* The same sweeps with one thread in the order the GPU row-action mode runs
+ * them: for each view, the rays nr = phase, phase + phases, ... for phase =
+ * 0 .. phases-1.  phases = 1 is the reference's own one-thread order. */
+void or_ms_solve_phased(const float *g, float *f, float *v, int iters, int phases) {
+    for (int i = 0; i < MS_IMG * MS_IMG; ++i) {
+        f[i] = 0.;
+        v[i] = 1.;
+    }
+    float lambda = 0.001;
+    int line[MS_IMG * 2];
+    float weight[MS_IMG * 2];
+    for (int it = 1; it <= iters; ++it) {
+        for (int j = 0; j < MS_NPROJ; ++j)
+            for (int ph = 0; ph < phases; ++ph)
+                for (int k = ph; k < MS_NRAY; k += phases) {
+                    int numb = or_ms_wray(j, k, line, weight);
+                    ms_min_image(g, f, v, lambda, j, k, line, weight, numb);
+                    ms_min_edge(f, v, lambda, line, numb);
+                }
+        lambda = lambda / (1 + 500 * lambda);
+    }
+}
+
 /* main.c:92-181: unit-pixel circle/bar phantom, values 0..3 */
 void or_ms_phantom(float *f) {
     memset(f, 0, sizeof(float) * MS_IMG * MS_IMG);

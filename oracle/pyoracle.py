@@ -110,6 +110,7 @@ def lib() -> C.CDLL:
         L.or_ms_A.argtypes = [_fp32, _fp32]
         L.or_ms_solve.argtypes = [_fp32, _fp32, _fp32, C.c_int, C.c_int]
         L.or_ms_phantom.argtypes = [_fp32]
+        L.or_ms_solve_phased.argtypes = [_fp32, _fp32, _fp32, C.c_int, C.c_int]
         L.or_cone_theta.argtypes = [C.POINTER(ConeGeom), C.c_int]
         L.or_cone_theta.restype = C.c_float
         L.or_cone_endpoints.argtypes = [C.POINTER(ConeGeom), C.c_int, C.c_int, C.c_int, _fp32, _fp32]
@@ -371,6 +372,15 @@ def ms_A(img: np.ndarray) -> np.ndarray:
     g = np.zeros((MS_NPROJ, MS_NRAY), np.float32)
     lib().or_ms_A(g, np.ascontiguousarray(img, np.float32))
     return g
+
+
+def ms_solve_phased(g: np.ndarray, iters: int = 10, phases: int = 4):
+    """One thread, rays of each view in `phases` interleaved groups (the GPU
+    row-action order); phases = 1 is msbeam's own one-thread order."""
+    f = np.zeros((MS_N, MS_N), np.float32)
+    v = np.ones((MS_N, MS_N), np.float32)
+    lib().or_ms_solve_phased(np.ascontiguousarray(g, np.float32), f, v, iters, phases)
+    return f, v
 
 
 def ms_solve(g: np.ndarray, iters: int = 10, nthreads: int = 0):

@@ -338,26 +338,34 @@ def run_ours(args):
 def run_serving(mg, n_requests: int, seed: int = 5):
     """C5-style serving sample: seeded requests with Poisson arrivals, served by
     the continuous-batching server and again one request at a time.  The mix is
-    the 2D part of C5 (78 % 256^2/512^2 slices with 360-720 views and 512-888
-    detectors, 22 % 1024^2 slices with 1440 views x 1536 detectors), 20-50
-    outer iterations each; the cone-beam share is not part of this engine yet."""
+    C5's: 256^2/512^2 slices with 360-720 views and 512-888 detectors, 1024^2
+    slices with 1440 views x 1536 detectors (about 22 %), and every tenth
+    request a 256^3 cone-beam volume with 360 projections of 384 x 512 cells;
+    20-50 outer iterations each."""
     rng = np.random.default_rng(np.random.PCG64(seed))
     G = mg.FanGeometry.covering
     small = [G(256, 1.0, 360, 512), G(256, 1.0, 720, 888), G(512, 0.75, 720, 888), G(512, 0.75, 360, 512)]
     large = G(1024, 0.375, 1440, 1536)
+    cone = mg.ConeGeometry(256, 256, 256, 0.4, 360, 384, 512, 0.8, 600.0, 1000.0)
     plans = {}
 
     def plan_of(g):
-        key = (g.n, g.nviews, g.ndets)
+        key = repr(g)
         if key not in plans:
-            plans[key] = mg.Plan.fan(g)
+            plans[key] = mg.Plan.cone(g) if isinstance(g, mg.ConeGeometry) else mg.Plan.fan(g)
         return plans[key]
 
     reqs = []
     for i in range(n_requests):
-        g = large if rng.uniform() < 0.22 else small[int(rng.integers(len(small)))]
-        p = plan_of(g)
-        ph = mg.phantom.ellipse_phantom(g.n, seed=7000 + i, n_random=int(rng.integers(0, 20)))
+        u = rng.uniform()
+        if i % 10 == 5:
+            g = cone
+            p = plan_of(g)
+            ph = mg.phantom.csg_phantom(256, 256, seed=7000 + i)
+        else:
+            g = large if u < 0.22 else small[int(rng.integers(len(small)))]
+            p = plan_of(g)
+            ph = mg.phantom.ellipse_phantom(g.n, seed=7000 + i, n_random=int(rng.integers(0, 20)))
         sino = mg.phantom.poisson_sinogram(p.forward(ph), float(rng.uniform(2e3, 2e4)), 8000 + i)
         reqs.append((p, sino, int(rng.integers(20, 51)), ph))
     # arrivals: Poisson, mean gap a third of the mean request time alone
@@ -385,7 +393,8 @@ def run_serving(mg, n_requests: int, seed: int = 5):
     same = all(np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
                for a, b in zip(results["continuous"], results["one_at_a_time"]))
     psnr = [mg.phantom.psnr(r[0], q[3]) for r, q in zip(results["continuous"], reqs)]
-    out.update({"requests": n_requests, "mix": "2D part of C5: 78% 256^2/512^2, 22% 1024^2 (1440x1536)",
+    out.update({"requests": n_requests, "mix": "C5: 256^2/512^2 slices, ~22% 1024^2 (1440x1536), every tenth a "
+                                                "256^3 cone volume (360 x 384 x 512)",
                 "iterations": "20-50 outer per request", "budget_gb": 150,
                 "results_identical_alone_vs_mix": bool(same), "psnr_db_median": round(float(np.median(psnr)), 3),
                 "speedup_slices_per_s": round(out["continuous"]["slices_per_s"] /
@@ -512,6 +521,29 @@ def run_openmp_equal_psnr(mg, st, tstream, batch: int, reps: int = 3):
     for _ in range(reps):
         f_e2e, _ = mg.reconstruct(plan, prm, sino)
     e2e = reps / (time.perf_counter() - t0)
+    # the same algorithm as msbeam on the GPU (row-action mode, 10 sweeps, data
+    # from msbeam's projection on the GPU), alone and in batches of `batch`
+    ra = mg.RowAction()
+    ra_rate, ra_psnr = {}, None
+    d_ph = torch.from_numpy(ph).cuda()
+    d_g1 = torch.empty((1, 180, 768), dtype=torch.float32, device="cuda")
+    ra.forward_dev(1, d_ph.data_ptr(), d_g1.data_ptr(), stream=st)
+    torch.cuda.synchronize()
+    for B in (1, batch):
+        d_g = d_g1.repeat(B, 1, 1).contiguous()
+        d_f = torch.empty((B, 512, 512), dtype=torch.float32, device="cuda")
+        d_v = torch.empty_like(d_f)
+        ra.run_dev(B, d_g.data_ptr(), d_f.data_ptr(), d_v.data_ptr(), stream=st)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(tstream)
+        ra.run_dev(B, d_g.data_ptr(), d_f.data_ptr(), d_v.data_ptr(), stream=st)
+        e1.record(tstream)
+        torch.cuda.synchronize()
+        ra_rate[B] = B / (e0.elapsed_time(e1) / 1e3)
+        if B == 1:
+            ra_psnr = mg.phantom.psnr(d_f[0].cpu().numpy(), ph, peak)
+    ra.close()
     cpu_rate = 1.0 / cpu_s
     return {
         "reference": f"msbeam/CPU_OpenMP restated (oracle/or_msbeam.c), OpenMP {cores} threads, 10 sweeps",
@@ -526,6 +558,12 @@ def run_openmp_equal_psnr(mg, st, tstream, batch: int, reps: int = 3):
                 f"slices_per_s_batch{batch}": round(rates["batched"], 2),
                 "slices_per_s_e2e_host_call": round(e2e, 2),
                 "l2": "flushed before every timed run"},
+        "gpu_row_action": {"algorithm": "msbeam's row-action AT on the GPU (at_rowaction_run), 10 sweeps, rays of a "
+                                         "view in 4 interleaved groups",
+                           "psnr_db": round(float(ra_psnr), 3), "slices_per_s_plain": round(ra_rate[1], 2),
+                           f"slices_per_s_batch{batch}": round(ra_rate[batch], 2),
+                           "speedup_plain": round(ra_rate[1] / cpu_rate, 1),
+                           "speedup_batched": round(ra_rate[batch] / cpu_rate, 1)},
         "speedup_plain": round(rates["plain"] / cpu_rate, 1),
         "speedup_batched": round(rates["batched"] / cpu_rate, 1),
         "speedup_e2e": round(e2e / cpu_rate, 1),

@@ -227,6 +227,8 @@ int at_rowaction_segments(const at_rowaction *ra, int64_t *segments);
 /* pixels (index y*n + x as msbeam addresses them) and weights of one ray */
 int at_rowaction_trace(const at_rowaction *ra, int32_t view, int32_t ray, int32_t *h_pix, float *h_w, int32_t cap,
                        int32_t *n_out);
+/* msbeam's projection A (proj.c:14-32) on the same traces: d_g = A d_f */
+int at_rowaction_forward(const at_rowaction *ra, int32_t nslices, const float *d_f, float *d_g, void *stream);
 /* f = 0, v = 1, then the sweeps (main.c:364-394); device buffers on `stream` */
 int at_rowaction_run(const at_rowaction *ra, int32_t nslices, const float *d_g, float *d_f, float *d_v,
                      const at_rowaction_params *prm, void *stream);

@@ -9,7 +9,7 @@
 // rays that are `phases` apart never touch each other's pixels or their
 // four neighbours (checked on every ray of msbeam's geometry for 3 and more),
 // so the rays nr = phase, phase + phases, ... of one view run concurrently,
-// one warp per ray, and views and phases follow one another.  The result is
+// one CTA per ray, and views and phases follow one another.  The result is
 // deterministic, and equal (up to the order of the ray sum) to one thread
 // running the rays in that order.
 //
@@ -172,15 +172,17 @@ struct RaArgs {
   double beta4e, betaeps;        // beta / (4 epsilon), beta * epsilon
 };
 
-constexpr int kRaWarps = 4;
-constexpr int kRaMaxSeg = 2048;  // per ray: at most 2n pixels, n <= 1024
+constexpr int kRaWarps = 4;       // rays per CTA of the forward projection
+constexpr int kRaThreads = 256;   // threads per ray of a sweep step
+constexpr int kRaMaxSeg = 2048;   // per ray: at most 2n pixels, n <= 1024
 
-// one warp per ray of (view, phase); blockIdx.y = slice
-__global__ void __launch_bounds__(32 * kRaWarps) ra_step_kernel(const RaArgs A) {
-  __shared__ float dbuf[kRaWarps][kRaMaxSeg];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int k = blockIdx.x * kRaWarps + warp;
-  if (k >= A.rays_in_phase) return;
+// one CTA per ray of (view, phase), its pixels spread over the threads;
+// blockIdx.y = slice
+__global__ void __launch_bounds__(kRaThreads) ra_step_kernel(const RaArgs A) {
+  __shared__ float d[kRaMaxSeg];
+  __shared__ float part[kRaThreads / 32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int k = blockIdx.x;
   const int nr = A.phase + k * A.phases;
   const int n = A.G.n, ray = A.view * A.G.nray + nr;
   const int64_t o0 = A.off[ray], o1 = A.off[ray + 1];
@@ -189,19 +191,26 @@ __global__ void __launch_bounds__(32 * kRaWarps) ra_step_kernel(const RaArgs A) 
   const float *wgt = A.weight + o0;
   float *f = A.f + (size_t)blockIdx.y * n * n;
   float *v = A.v + (size_t)blockIdx.y * n * n;
-  float *d = dbuf[warp];
-  // minIMAGE, main.c:213-261
+  // minIMAGE, main.c:213-261: the ray's projection, summed in a fixed tree
   float af = 0.f;
-  for (int i = lane; i < numb; i += 32) af = __fadd_rn(af, __fmul_rn(f[line[i]], wgt[i]));
+  for (int i = tid; i < numb; i += kRaThreads) af = __fadd_rn(af, __fmul_rn(f[line[i]], wgt[i]));
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) af = __fadd_rn(af, __shfl_xor_sync(0xffffffffu, af, o));
+  if (lane == 0) part[warp] = af;
+  __syncthreads();
+  af = 0.f;
+#pragma unroll
+  for (int w = 0; w < kRaThreads / 32; w++) af = __fadd_rn(af, part[w]);
   af = __fsub_rn(af, A.g[(size_t)blockIdx.y * A.G.nproj * A.G.nray + ray]);
-  for (int i = lane; i < numb; i += 32) {
+  for (int i = tid; i < numb; i += kRaThreads) {
     const int ind = line[i], x = ind / n, y = ind % n;
     const float fc = f[ind], vc = v[ind], vc2 = __fmul_rn(vc, vc);
     float tmp = 0.f, lap = 0.f;
-    tmp = __fadd_rn(tmp, __fmul_rn(vc2, __fsub_rn(x + 1 < n ? f[ind + n] : 0.f, fc)));
-    tmp = __fadd_rn(tmp, __fmul_rn(vc2, __fsub_rn(y + 1 < n ? f[ind + 1] : 0.f, fc)));
+    float fd = 0.f, fr = 0.f;  // neighbours past the edge are zero (never read)
+    if (x + 1 < n) fd = f[ind + n];
+    if (y + 1 < n) fr = f[ind + 1];
+    tmp = __fadd_rn(tmp, __fmul_rn(vc2, __fsub_rn(fd, fc)));
+    tmp = __fadd_rn(tmp, __fmul_rn(vc2, __fsub_rn(fr, fc)));
     if (x - 1 >= 0) tmp = __fsub_rn(tmp, __fmul_rn(__fmul_rn(v[ind - n], v[ind - n]), __fsub_rn(fc, f[ind - n])));
     else tmp = __fsub_rn(tmp, __fsub_rn(fc, 0.f));
     if (y - 1 >= 0) tmp = __fsub_rn(tmp, __fmul_rn(__fmul_rn(v[ind - 1], v[ind - 1]), __fsub_rn(fc, f[ind - 1])));
@@ -213,20 +222,23 @@ __global__ void __launch_bounds__(32 * kRaWarps) ra_step_kernel(const RaArgs A) 
     lap = __fsub_rn(lap, __fmul_rn(4.f, fc));
     d[i] = __fadd_rn(__fmul_rn(-af, wgt[i]), __fmul_rn(A.alpha, __fadd_rn(tmp, __fmul_rn(A.eps2, lap))));
   }
-  __syncwarp();
-  for (int i = lane; i < numb; i += 32) {
+  __syncthreads();  // every read of f before any write (main.c:255-260 updates after the loop)
+  for (int i = tid; i < numb; i += kRaThreads) {
     const int ind = line[i];
     float fn = __fadd_rn(f[ind], __fmul_rn(A.lambda, d[i]));
     f[ind] = fn < 0 ? 0.f : fn;
   }
-  __syncwarp();
+  __syncthreads();
   // minEDGE, main.c:263-301
-  for (int i = lane; i < numb; i += 32) {
+  for (int i = tid; i < numb; i += kRaThreads) {
     const int ind = line[i], x = ind / n, y = ind % n;
     const float fc = f[ind], vc = v[ind];
     float a = 0.f, c = 0.f;
-    const float gx = __fsub_rn(fc, x - 1 >= 0 ? f[ind - n] : 0.f);
-    const float gy = __fsub_rn(fc, y - 1 >= 0 ? f[ind - 1] : 0.f);
+    float fu = 0.f, fl = 0.f;
+    if (x - 1 >= 0) fu = f[ind - n];
+    if (y - 1 >= 0) fl = f[ind - 1];
+    const float gx = __fsub_rn(fc, fu);
+    const float gy = __fsub_rn(fc, fl);
     a = __fadd_rn(a, __fmul_rn(gx, gx));
     a = __fadd_rn(a, __fmul_rn(gy, gy));
     a = __fmul_rn(a, vc);
@@ -241,13 +253,28 @@ __global__ void __launch_bounds__(32 * kRaWarps) ra_step_kernel(const RaArgs A) 
                                 __dmul_rn(A.betaeps, (double)c));
     d[i] = __double2float_rn(dd);
   }
-  __syncwarp();
-  for (int i = lane; i < numb; i += 32) {
+  __syncthreads();
+  for (int i = tid; i < numb; i += kRaThreads) {
     const int ind = line[i];
     float vn = __fadd_rn(v[ind], __fmul_rn(A.lambda, d[i]));
     vn = vn < 0 ? 0.f : vn;
     v[ind] = vn > 1 ? 1.f : vn;
   }
+}
+
+// msbeam's A (proj.c:14-32) on its traces: g[ray] = sum f[pixel] * weight,
+// a warp per ray (the sum in tree order); blockIdx.y = slice
+__global__ void __launch_bounds__(32 * kRaWarps) ra_forward_kernel(const RaGeom G, const int64_t *off, const int *line,
+                                                                 const float *weight, const float *f, float *g) {
+  const int ray = blockIdx.x * kRaWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  const int rays = G.nproj * G.nray;
+  if (ray >= rays) return;
+  const float *fs = f + (size_t)blockIdx.y * G.n * G.n;
+  float acc = 0.f;
+  for (int64_t i = off[ray] + lane; i < off[ray + 1]; i += 32) acc = __fadd_rn(acc, __fmul_rn(fs[line[i]], weight[i]));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc = __fadd_rn(acc, __shfl_xor_sync(0xffffffffu, acc, o));
+  if (lane == 0) g[(size_t)blockIdx.y * rays + ray] = acc;
 }
 
 __global__ void ra_init_kernel(float *f, float *v, size_t n) {
@@ -342,6 +369,16 @@ AT_API int at_rowaction_trace(const at_rowaction *ra, int32_t view, int32_t ray,
   return AT_OK;
 }
 
+AT_API int at_rowaction_forward(const at_rowaction *ra, int32_t nslices, const float *d_f, float *d_g, void *stream) {
+  if (!ra || !d_f || !d_g) return set_error(AT_EINVAL, "at_rowaction_forward: null argument");
+  if (nslices < 1 || nslices > 65535) return set_error(AT_EINVAL, "at_rowaction_forward: nslices must be in [1, 65535]");
+  const int rays = ra->G.nproj * ra->G.nray;
+  dim3 grid((rays + kRaWarps - 1) / kRaWarps, nslices);
+  ra_forward_kernel<<<grid, 32 * kRaWarps, 0, (cudaStream_t)stream>>>(ra->G, ra->off, ra->line, ra->weight, d_f, d_g);
+  AT_CUDA_TRY(cudaGetLastError());
+  return AT_OK;
+}
+
 AT_API int at_rowaction_run(const at_rowaction *ra, int32_t nslices, const float *d_g, float *d_f, float *d_v,
                             const at_rowaction_params *prm, void *stream) {
   if (!ra || !d_g || !d_f || !d_v || !prm) return set_error(AT_EINVAL, "at_rowaction_run: null argument");
@@ -375,8 +412,8 @@ AT_API int at_rowaction_run(const at_rowaction *ra, int32_t nslices, const float
         A.view = view;
         A.phase = ph;
         A.rays_in_phase = (ra->G.nray - ph + prm->phases - 1) / prm->phases;
-        dim3 grid((A.rays_in_phase + kRaWarps - 1) / kRaWarps, nslices);
-        ra_step_kernel<<<grid, 32 * kRaWarps, 0, st>>>(A);
+        dim3 grid(A.rays_in_phase, nslices);
+        ra_step_kernel<<<grid, kRaThreads, 0, st>>>(A);
       }
     AT_CUDA_TRY(cudaGetLastError());
     lambda = lambda / (1 + prm->lambda_decay * lambda);  // main.c:391

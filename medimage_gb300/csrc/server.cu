@@ -12,7 +12,8 @@
 //
 // Each request's arithmetic depends only on its own data and geometry (the
 // projector variant is fixed for the server's lifetime), so its result is the
-// same alone and in any mix.
+// same alone and in any mix.  Fan-beam and ray-table slices share one batch,
+// cone-beam volumes another; a round advances both.
 #include <algorithm>
 #include <chrono>
 #include <cstring>
@@ -67,7 +68,8 @@ struct Server {
   std::map<int64_t, std::unique_ptr<Request>> reqs;
   std::vector<Request *> pending;  // arrival order
   std::vector<Request *> active;
-  Batch batch;
+  Batch batch[2];  // 0: fan beam and ray tables, 1: cone beam
+  bool has[2] = {false, false};
   bool dirty = true;
   int64_t next_id = 1;
   size_t used = 0, peak = 0;
@@ -146,13 +148,19 @@ struct Server {
         continue;
       }
       if (dirty) {
-        std::vector<ScanDev> scans;
-        for (auto *r : active) scans.push_back(r->dev);
-        if ((rc = batch.set(scans.data(), (int)scans.size(), AT_GEOM_FAN, rpt, st))) return rc;
+        std::vector<ScanDev> scans[2];
+        for (auto *r : active) scans[r->plan->kind == AT_GEOM_CONE ? 1 : 0].push_back(r->dev);
+        for (int k = 0; k < 2; k++) {
+          has[k] = !scans[k].empty();
+          if (has[k] && (rc = batch[k].set(scans[k].data(), (int)scans[k].size(), k ? AT_GEOM_CONE : AT_GEOM_FAN,
+                                           rpt, st)))
+            return rc;
+        }
         dirty = false;
       }
       const double r0 = now_s();
-      if ((rc = batch.enqueue_outer(st))) return rc;
+      for (int k = 0; k < 2; k++)
+        if (has[k] && (rc = batch[k].enqueue_outer(st))) return rc;
       AT_CUDA_TRY(cudaStreamSynchronize(st));
       const double r1 = now_s();
       busy += r1 - r0;
@@ -190,7 +198,7 @@ AT_API int at_server_create(const at_server_config *cfg, at_server **out) {
   auto S = std::make_unique<at_server>();
   S->s.cfg = *cfg;
   S->s.prm = at_params{cfg->alpha, cfg->beta, cfg->epsilon, 0, cfg->iter_image, cfg->iter_edge, cfg->mode};
-  S->s.batch.params = S->s.prm;
+  for (auto &b : S->s.batch) b.params = S->s.prm;
   S->s.rpt = cfg->fp_rays_per_thread > 0 ? cfg->fp_rays_per_thread : 1;
   if (S->s.rpt != 1 && S->s.rpt != 2 && S->s.rpt != 4)
     return set_error(AT_EINVAL, "at_server_create: fp_rays_per_thread must be 1, 2 or 4");
@@ -205,8 +213,8 @@ AT_API void at_server_destroy(at_server *s) { delete s; }
 AT_API int at_server_submit(at_server *srv, at_plan *plan, const float *h_sino, int32_t iter_alt, double arrival_s,
                             int64_t *id) {
   if (!srv || !plan || !h_sino || !id) return set_error(AT_EINVAL, "at_server_submit: null argument");
-  if (plan->p.kind == AT_GEOM_GOLDNC || plan->p.kind == AT_GEOM_CONE)
-    return set_error(AT_EINVAL, "at_server_submit: fan-beam and ray-table plans only");
+  if (plan->p.kind == AT_GEOM_GOLDNC)
+    return set_error(AT_EINVAL, "at_server_submit: fan-beam, ray-table and cone-beam plans only");
   if (iter_alt < 1) return set_error(AT_EINVAL, "at_server_submit: iter_alt must be >= 1");
   Server &S = srv->s;
   if (scan_bytes(plan->p, S.rpt) > S.cfg.hbm_budget_bytes)

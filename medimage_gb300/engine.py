@@ -119,6 +119,7 @@ SIGNATURES = {
     "at_rowaction_destroy": ([C.c_void_p], None),
     "at_rowaction_segments": ([C.c_void_p, C.POINTER(C.c_int64)], C.c_int),
     "at_rowaction_trace": ([C.c_void_p, C.c_int32, C.c_int32, _ip, _fp, C.c_int32, C.POINTER(C.c_int32)], C.c_int),
+    "at_rowaction_forward": ([C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
     "at_rowaction_run": ([C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(_RowActionParams),
                           C.c_void_p], C.c_int),
     "at_plan_create_cone": ([C.POINTER(_ConeGeom), C.POINTER(C.c_void_p)], C.c_int),
@@ -638,6 +639,30 @@ class RowAction:
         k = C.c_int32()
         _check("at_rowaction_trace", lib().at_rowaction_trace(self._h, view, ray, pix, w, cap, C.byref(k)))
         return pix[: k.value].copy(), w[: k.value].copy()
+
+    def forward_dev(self, nslices: int, d_f: int, d_g: int, stream: int = 0) -> None:
+        _check("at_rowaction_forward", lib().at_rowaction_forward(self._h, nslices, C.c_void_p(d_f), C.c_void_p(d_g),
+                                                                  C.c_void_p(stream)))
+
+    def forward(self, f: np.ndarray) -> np.ndarray:
+        """msbeam's projection of an n x n image (host arrays)."""
+        f = np.ascontiguousarray(f, np.float32)
+        L = lib()
+        ptr = []
+        try:
+            for nbytes in (f.nbytes, self.nproj * self.nray * 4):
+                p = C.c_void_p()
+                _check("at_dev_alloc", L.at_dev_alloc(C.byref(p), nbytes))
+                ptr.append(p.value)
+            _check("h2d", L.at_memcpy_h2d(C.c_void_p(ptr[0]), f.ctypes.data, f.nbytes, None))
+            self.forward_dev(1, ptr[0], ptr[1])
+            g = np.zeros((self.nproj, self.nray), np.float32)
+            _check("d2h", L.at_memcpy_d2h(g.ctypes.data, C.c_void_p(ptr[1]), g.nbytes, None))
+            _check("sync", L.at_stream_sync(None))
+        finally:
+            for p in ptr:
+                L.at_dev_free(C.c_void_p(p))
+        return g
 
     def run_dev(self, nslices: int, d_g: int, d_f: int, d_v: int, params: RowActionParams | None = None,
                 stream: int = 0) -> None:

@@ -31,6 +31,15 @@ def test_traces_equal_msbeam(ra, oracle):
             np.testing.assert_array_equal(wg.view(np.uint32), w[:n].view(np.uint32), err_msg=f"ray ({view},{ray})")
 
 
+def test_forward_matches_msbeam(ra, oracle):
+    """msbeam sums each ray sequentially in FP32, the GPU in a tree: the
+    projector bar of rel-L2 1e-5 applies."""
+    ph = oracle.ms_phantom()
+    g = ra.forward(ph)
+    ref = oracle.ms_A(ph)
+    assert np.linalg.norm(g - ref) / np.linalg.norm(ref) <= 1e-5
+
+
 def test_sweeps_match_oracle_order(engine, ra, oracle):
     ph = oracle.ms_phantom()
     g = oracle.ms_A(ph)

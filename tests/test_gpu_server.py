@@ -61,3 +61,27 @@ def test_server_admission_respects_budget(engine, oracle):
     with pytest.raises(engine.AtError) as ei:
         tiny.submit(plans[0], reqs[0][1], 2, 0.0)
     assert ei.value.code == -5
+
+
+def test_server_mixes_slices_and_cone_volumes(engine, oracle):
+    """Cone-beam volumes run in the same rounds as fan-beam slices (a second
+    batch); each result equals the request served alone, bitwise."""
+    plans, reqs = make_requests(engine, oracle)
+    cg = engine.ConeGeometry(32, 32, 24, 1.0, 40, 28, 36, 1.6, 80.0, 150.0)
+    cp = engine.Plan.cone(cg)
+    for i in range(2):
+        vol = engine.phantom.csg_phantom(32, 24, seed=70 + i, n_parts=5, n_voids=4)
+        reqs.insert(2 * i + 1, (cp, cp.forward(vol), 2 + i, 0.001 * (2 * i + 1)))
+    srv = engine.Server(hbm_budget_bytes=1 << 34, max_active=4)
+    ids = [srv.submit(p, s, it, arr) for (p, s, it, arr) in reqs]
+    srv.run()
+    assert srv.stats()["completed"] == len(reqs)
+    for rid, (p, s, it, _) in zip(ids, reqs):
+        f_mix, v_mix, _, _ = srv.result(rid)
+        alone = engine.Server(hbm_budget_bytes=1 << 34, max_active=1)
+        a = alone.submit(p, s, it, 0.0)
+        alone.run()
+        f_one, v_one, _, _ = alone.result(a)
+        assert f_mix.shape == p.img_shape
+        np.testing.assert_array_equal(f_mix, f_one)
+        np.testing.assert_array_equal(v_mix, v_one)

@@ -2,18 +2,19 @@
 //
 // Requests (a plan, a sinogram, an outer-iteration count, an arrival time)
 // are admitted into a running batch as soon as they have arrived and their
-// device state fits the HBM admission budget and a slot is free.  Every round
-// advances all admitted requests by one outer iteration (image step + edge
-// step of origin/GoldenC/src/main.c:43-47) with one launch per kernel for the
-// whole mix, so the work of different requests overlaps on the device.  A
+// device state fits the HBM admission budget and a slot is free.  The requests
+// of one geometry form a batch on its own stream; a round advances all of them
+// by one outer iteration (image step + edge step of
+// origin/GoldenC/src/main.c:43-47) with one launch per kernel, and the rounds
+// of different geometries run concurrently, so the work of different requests
+// overlaps on the device.  A
 // request leaves the batch after its last iteration: f and v are copied out,
 // its state is freed and its slot goes to the next request.  Sinogram, f, v
 // and the CG state stay in HBM from admission to completion.
 //
 // Each request's arithmetic depends only on its own data and geometry (the
 // projector variant is fixed for the server's lifetime), so its result is the
-// same alone and in any mix.  Fan-beam and ray-table slices share one batch,
-// cone-beam volumes another; a round advances both.
+// same alone and in any mix.
 #include <algorithm>
 #include <chrono>
 #include <cstring>
@@ -60,17 +61,34 @@ struct Request {
   std::vector<float> f, v;
 };
 
+// The requests of one geometry: one batch, advanced one outer iteration per
+// round on its own stream, so requests of a slow geometry (a cone volume, a
+// 1024^2 slice) do not hold back those of a fast one; the GPU runs the groups'
+// rounds concurrently.
+struct Group {
+  Plan *plan = nullptr;
+  Batch batch;
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev = nullptr;
+  std::vector<Request *> active;
+  std::vector<Request *> round;  // the requests the round in flight advances
+  bool dirty = true, in_flight = false;
+  double r0 = 0.0;
+  ~Group() {
+    if (ev) cudaEventDestroy(ev);
+    if (st) cudaStreamDestroy(st);
+  }
+};
+
 struct Server {
   at_server_config cfg{};
   at_params prm{};
   int rpt = 1;
-  cudaStream_t st = nullptr;
+  cudaStream_t st = nullptr;  // the caller-side stream (creation only)
   std::map<int64_t, std::unique_ptr<Request>> reqs;
   std::vector<Request *> pending;  // arrival order
-  std::vector<Request *> active;
-  Batch batch[2];  // 0: fan beam and ray tables, 1: cone beam
-  bool has[2] = {false, false};
-  bool dirty = true;
+  std::map<const Plan *, std::unique_ptr<Group>> groups;
+  int nactive = 0;
   int64_t next_id = 1;
   size_t used = 0, peak = 0;
   int64_t rounds = 0, completed = 0;
@@ -78,39 +96,61 @@ struct Server {
   int64_t slices = 0;
 
   ~Server() {
+    for (auto &kv : groups) cudaStreamSynchronize(kv.second->st);
     for (auto &kv : reqs)
       if (kv.second->mem) cudaFree(kv.second->mem);
+    groups.clear();
     if (st) cudaStreamDestroy(st);
   }
 
+  int group_of(Plan *plan, Group **out) {
+    auto &g = groups[plan];
+    if (!g) {
+      g = std::make_unique<Group>();
+      g->plan = plan;
+      g->batch.params = prm;
+      AT_CUDA_TRY(cudaStreamCreateWithFlags(&g->st, cudaStreamNonBlocking));
+      AT_CUDA_TRY(cudaEventCreateWithFlags(&g->ev, cudaEventDisableTiming));
+    }
+    *out = g.get();
+    return AT_OK;
+  }
+
   int admit(Request *r, double t) {
+    Group *g = nullptr;
+    int rc = group_of(r->plan, &g);
+    if (rc) return rc;
+    cudaStream_t gs = g->st;
     r->bytes = scan_bytes(*r->plan, rpt);
-    cudaError_t e = cudaMallocAsync(&r->mem, r->bytes, st);
+    cudaError_t e = cudaMallocAsync(&r->mem, r->bytes, gs);
     if (e != cudaSuccess) return cuda_error(e, "server: state allocation");
     carve_scan(r->dev, *r->plan, rpt, (char *)r->mem);
     r->ctl = make_ctl(prm);
-    AT_CUDA_TRY(cudaMemcpyAsync(r->dev.ctl, &r->ctl, sizeof(Ctl), cudaMemcpyHostToDevice, st));
+    AT_CUDA_TRY(cudaMemcpyAsync(r->dev.ctl, &r->ctl, sizeof(Ctl), cudaMemcpyHostToDevice, gs));
     AT_CUDA_TRY(cudaMemcpyAsync(r->dev.buf[B_G], r->sino.data(), sizeof(float) * r->sino.size(),
-                                cudaMemcpyHostToDevice, st));
-    AT_CUDA_TRY(cudaMemsetAsync(r->dev.buf[B_F], 0, sizeof(float) * r->dev.npix, st));  // main.c:36
-    AT_CUDA_TRY(launch_fill(r->dev.buf[B_V], 1.f, r->dev.npix, st));                   // main.c:37-40
-    if (const size_t bpb = bp_scratch_bytes(*r->plan)) AT_CUDA_TRY(cudaMemsetAsync(r->dev.bp_acc, 0, bpb, st));
+                                cudaMemcpyHostToDevice, gs));
+    AT_CUDA_TRY(cudaMemsetAsync(r->dev.buf[B_F], 0, sizeof(float) * r->dev.npix, gs));  // main.c:36
+    AT_CUDA_TRY(launch_fill(r->dev.buf[B_V], 1.f, r->dev.npix, gs));                   // main.c:37-40
+    if (const size_t bpb = bp_scratch_bytes(*r->plan)) AT_CUDA_TRY(cudaMemsetAsync(r->dev.bp_acc, 0, bpb, gs));
     used += r->bytes;
     peak = std::max(peak, used);
     r->state = 1;
     r->t_admit = t;
-    active.push_back(r);
-    dirty = true;
+    g->active.push_back(r);
+    g->dirty = true;
+    nactive++;
     return AT_OK;
   }
 
-  int retire(Request *r, double t) {
+  int retire(Group *g, Request *r, double t) {
     r->f.resize(r->dev.npix);
     r->v.resize(r->dev.npix);
-    AT_CUDA_TRY(cudaMemcpyAsync(r->f.data(), r->dev.buf[B_F], sizeof(float) * r->dev.npix, cudaMemcpyDeviceToHost, st));
-    AT_CUDA_TRY(cudaMemcpyAsync(r->v.data(), r->dev.buf[B_V], sizeof(float) * r->dev.npix, cudaMemcpyDeviceToHost, st));
-    AT_CUDA_TRY(cudaFreeAsync(r->mem, st));
-    AT_CUDA_TRY(cudaStreamSynchronize(st));
+    AT_CUDA_TRY(cudaMemcpyAsync(r->f.data(), r->dev.buf[B_F], sizeof(float) * r->dev.npix, cudaMemcpyDeviceToHost,
+                                g->st));
+    AT_CUDA_TRY(cudaMemcpyAsync(r->v.data(), r->dev.buf[B_V], sizeof(float) * r->dev.npix, cudaMemcpyDeviceToHost,
+                                g->st));
+    AT_CUDA_TRY(cudaFreeAsync(r->mem, g->st));
+    AT_CUDA_TRY(cudaStreamSynchronize(g->st));
     r->mem = nullptr;
     used -= r->bytes;
     r->state = 2;
@@ -119,8 +159,9 @@ struct Server {
     r->sino.shrink_to_fit();
     completed++;
     slices++;
+    nactive--;
     t_last = std::max(t_last, t);
-    dirty = true;
+    g->dirty = true;
     return AT_OK;
   }
 
@@ -128,52 +169,66 @@ struct Server {
     if (t0 < 0) t0 = now_s();
     const double start = now_s();
     int rc;
-    while (!pending.empty() || !active.empty()) {
+    while (!pending.empty() || nactive > 0) {
       const double t = now_s() - t0;
       if (now_s() - start > max_seconds) break;
       // admission: arrived requests in order, while slots and budget allow
-      while (!pending.empty() && pending.front()->arrival <= t && (int)active.size() < cfg.max_active) {
+      while (!pending.empty() && pending.front()->arrival <= t && nactive < cfg.max_active) {
         Request *r = pending.front();
         if (used + scan_bytes(*r->plan, rpt) > cfg.hbm_budget_bytes) {
-          if (active.empty()) return set_error(AT_EBUDGET, "server: request does not fit the HBM budget");
+          if (nactive == 0) return set_error(AT_EBUDGET, "server: request does not fit the HBM budget");
           break;
         }
         if ((rc = admit(r, t))) return rc;
         if (t_first < 0) t_first = r->arrival;
         pending.erase(pending.begin());
       }
-      if (active.empty()) {  // idle until the next arrival
+      if (nactive == 0) {  // idle until the next arrival
         const double wait = pending.front()->arrival - (now_s() - t0);
         if (wait > 0) std::this_thread::sleep_for(std::chrono::duration<double>(std::min(wait, 0.05)));
         continue;
       }
-      if (dirty) {
-        std::vector<ScanDev> scans[2];
-        for (auto *r : active) scans[r->plan->kind == AT_GEOM_CONE ? 1 : 0].push_back(r->dev);
-        for (int k = 0; k < 2; k++) {
-          has[k] = !scans[k].empty();
-          if (has[k] && (rc = batch[k].set(scans[k].data(), (int)scans[k].size(), k ? AT_GEOM_CONE : AT_GEOM_FAN,
-                                           rpt, st)))
+      // start a round in every idle group that has requests
+      for (auto &kv : groups) {
+        Group *g = kv.second.get();
+        if (g->in_flight || g->active.empty()) continue;
+        if (g->dirty) {
+          std::vector<ScanDev> scans;
+          for (auto *r : g->active) scans.push_back(r->dev);
+          if ((rc = g->batch.set(scans.data(), (int)scans.size(), g->plan->kind == AT_GEOM_CONE ? AT_GEOM_CONE
+                                                                                                 : AT_GEOM_FAN,
+                                 rpt, g->st)))
             return rc;
+          g->dirty = false;
         }
-        dirty = false;
+        g->r0 = now_s();
+        g->round = g->active;  // requests admitted during the round join the next one
+        if ((rc = g->batch.enqueue_outer(g->st))) return rc;
+        AT_CUDA_TRY(cudaEventRecord(g->ev, g->st));
+        g->in_flight = true;
       }
-      const double r0 = now_s();
-      for (int k = 0; k < 2; k++)
-        if (has[k] && (rc = batch[k].enqueue_outer(st))) return rc;
-      AT_CUDA_TRY(cudaStreamSynchronize(st));
-      const double r1 = now_s();
-      busy += r1 - r0;
-      rounds++;
-      std::vector<Request *> still;
-      for (auto *r : active) {
-        if (++r->iters_done >= r->iter_alt) {
-          if ((rc = retire(r, r1 - t0))) return rc;
-        } else {
-          still.push_back(r);
+      // finish the rounds that are done
+      bool progressed = false;
+      for (auto &kv : groups) {
+        Group *g = kv.second.get();
+        if (!g->in_flight) continue;
+        const cudaError_t q = cudaEventQuery(g->ev);
+        if (q == cudaErrorNotReady) continue;
+        AT_CUDA_TRY(q);
+        const double r1 = now_s();
+        busy += r1 - g->r0;
+        rounds++;
+        g->in_flight = false;
+        progressed = true;
+        for (auto *r : g->round) {
+          if (++r->iters_done >= r->iter_alt) {
+            if ((rc = retire(g, r, r1 - t0))) return rc;
+            g->active.erase(std::find(g->active.begin(), g->active.end(), r));
+          }
         }
+        g->round.clear();
       }
-      active.swap(still);
+      if (!progressed) std::this_thread::sleep_for(std::chrono::microseconds(50));
     }
     return AT_OK;
   }
@@ -198,7 +253,6 @@ AT_API int at_server_create(const at_server_config *cfg, at_server **out) {
   auto S = std::make_unique<at_server>();
   S->s.cfg = *cfg;
   S->s.prm = at_params{cfg->alpha, cfg->beta, cfg->epsilon, 0, cfg->iter_image, cfg->iter_edge, cfg->mode};
-  for (auto &b : S->s.batch) b.params = S->s.prm;
   S->s.rpt = cfg->fp_rays_per_thread > 0 ? cfg->fp_rays_per_thread : 1;
   if (S->s.rpt != 1 && S->s.rpt != 2 && S->s.rpt != 4)
     return set_error(AT_EINVAL, "at_server_create: fp_rays_per_thread must be 1, 2 or 4");

@@ -30,11 +30,51 @@ namespace at {
 // ---------------------------------------------------------------------------
 // fan-beam forward projection
 // ---------------------------------------------------------------------------
-template <int RPT>
+// A batch's scans that share one plan form a group (up to kGroupMax, listed in
+// the lead scan's ScanDev).  Their input images are first interleaved into the
+// lead's pack buffer (fp_pack_kernel, one float4 per pixel); the lead's CTAs
+// then walk each ray once and one 16-byte gather per segment feeds every
+// member, so the walk (decision bits, crossing arithmetic) and the gathers are
+// shared.  Each member's sum is formed exactly as it would be alone, so
+// results do not depend on the grouping.
+__global__ void __launch_bounds__(256) fp_pack_kernel(const Launch L) {
+  const int scan = find_scan(L.prefix, L.nscans, blockIdx.x);
+  const ScanDev &S = L.scans[scan];
+  if (S.nmem == 0) return;
+  const float *src[kGroupMax];
+  bool any = false;
+#pragma unroll
+  for (int m = 0; m < kGroupMax; m++) {
+    const ScanDev &Mm = L.scans[S.mem[m < S.nmem ? m : 0]];
+    src[m] = (m < S.nmem && flow_active(Mm, L.flow)) ? Mm.buf[L.in_buf] : nullptr;
+    any |= src[m] != nullptr;
+  }
+  if (!any) return;
+  const int cta0 = __ldg(L.prefix + scan), ncta = __ldg(L.prefix + scan + 1) - cta0;
+  const int npix = S.n * S.n;
+  for (int p = (blockIdx.x - cta0) * blockDim.x + threadIdx.x; p < npix; p += ncta * blockDim.x) {
+    float v[kGroupMax];
+#pragma unroll
+    for (int m = 0; m < kGroupMax; m++) v[m] = src[m] ? __ldg(src[m] + p) : 0.f;
+    S.pack[p] = make_float4(v[0], v[1], v[2], v[3]);
+  }
+}
+
+template <int RPT, int G>
 __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
   const int scan = L.scans ? find_scan(L.prefix, L.nscans, blockIdx.x) : 0;
   const ScanDev &S = scan_of(L, scan);
-  if (!flow_active(S, L.flow)) return;
+  const int nm = L.scans ? S.nmem : 1;
+  const ScanDev *M[G];
+  bool act[G];
+  bool any = false;
+#pragma unroll
+  for (int m = 0; m < G; m++) {
+    M[m] = L.scans ? &L.scans[S.mem[m < nm ? m : 0]] : &L.single;
+    act[m] = m < nm && flow_active(*M[m], L.flow);
+    any |= act[m];
+  }
+  if (!any) return;
   const int cta0 = L.scans ? __ldg(L.prefix + scan) : 0;
   const int ncta = L.scans ? __ldg(L.prefix + scan + 1) - cta0 : gridDim.x;
   const int local_cta = blockIdx.x - cta0;
@@ -43,15 +83,19 @@ __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
   const int lw = local_cta * 4 + (threadIdx.x >> 5);
   const int blk = lw / kWarpsPerBlock, slice = lw % kWarpsPerBlock;
   const int nblk = S.nviews * S.nbpv;
-  double s0 = 0.0;
+  double s0[G];
+#pragma unroll
+  for (int m = 0; m < G; m++) s0[m] = 0.0;
   if (blk < nblk) {
     const int view = blk / S.nbpv;
     const int in_blk = slice * 32 * RPT + lane * RPT;  // first ray of this thread within the block
     const int det0 = (blk % S.nbpv) * kRayBlock + in_blk;
-    const float *__restrict__ img = S.buf[L.in_buf];
+    static_assert(G == 1 || G == 4, "members are gathered as one float or one float4");
+    const float *__restrict__ img = M[0]->buf[L.in_buf];
+    const float4 *__restrict__ pack = S.pack;
     const unsigned npix = (unsigned)S.npix;
     int idx[RPT], stx[RPT], sty[RPT], nseg[RPT];
-    float ax[RPT], ay[RPT], lx[RPT], ly[RPT], cx[RPT], cy[RPT], prev[RPT], acc[RPT], comp[RPT];
+    float ax[RPT], ay[RPT], lx[RPT], ly[RPT], cx[RPT], cy[RPT], prev[RPT], acc[RPT][G], comp[RPT][G];
     int my_max = 0;
 #pragma unroll
     for (int r = 0; r < RPT; r++) {
@@ -72,7 +116,9 @@ __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
         lx[r] = __uint_as_float(h1.z);
         ly[r] = __uint_as_float(h1.w);
       }
-      cx[r] = cy[r] = prev[r] = acc[r] = comp[r] = 0.f;
+      cx[r] = cy[r] = prev[r] = 0.f;
+#pragma unroll
+      for (int m = 0; m < G; m++) acc[r][m] = comp[r][m] = 0.f;
       my_max = max(my_max, nseg[r]);
     }
     // warp-uniform trip count, and the words that are full for every ray
@@ -98,9 +144,11 @@ __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
       } else {
         bw[0] = __ldg(wp + (size_t)w * kRayBlock);
       }
-      float part[RPT];
+      float part[RPT][G];
 #pragma unroll
-      for (int r = 0; r < RPT; r++) part[r] = 0.f;
+      for (int r = 0; r < RPT; r++)
+#pragma unroll
+        for (int m = 0; m < G; m++) part[r][m] = 0.f;
       const int base = w << 5;
       if (w < wfull) {
         // every ray of the warp has 32 segments in this word and none of them
@@ -115,7 +163,15 @@ __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
             const float cur = bx ? nx : ny;
             const float wt = cur - prev[r];
             prev[r] = cur;
-            part[r] = fmaf(wt, __ldg(img + idx[r]), part[r]);
+            if constexpr (G == 1) {
+              part[r][0] = fmaf(wt, __ldg(img + idx[r]), part[r][0]);
+            } else {
+              const float4 v = __ldg(pack + idx[r]);
+              part[r][0] = fmaf(wt, v.x, part[r][0]);
+              part[r][1] = fmaf(wt, v.y, part[r][1]);
+              part[r][2] = fmaf(wt, v.z, part[r][2]);
+              part[r][3] = fmaf(wt, v.w, part[r][3]);
+            }
             idx[r] += bx ? stx[r] : sty[r];
             cx[r] += bx ? 1.f : 0.f;
             cy[r] += bx ? 0.f : 1.f;
@@ -133,8 +189,18 @@ __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
             const float wt = cur - prev[r];
             prev[r] = cur;
             const bool on = (base + b) < nseg[r] && (unsigned)idx[r] < npix;
-            const float val = on ? __ldg(img + idx[r]) : 0.f;
-            part[r] = fmaf(wt, val, part[r]);
+            if constexpr (G == 1) {
+              float val = 0.f;
+              if (on) val = __ldg(img + idx[r]);
+              part[r][0] = fmaf(wt, val, part[r][0]);
+            } else {
+              float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+              if (on) v = __ldg(pack + idx[r]);
+              part[r][0] = fmaf(wt, v.x, part[r][0]);
+              part[r][1] = fmaf(wt, v.y, part[r][1]);
+              part[r][2] = fmaf(wt, v.z, part[r][2]);
+              part[r][3] = fmaf(wt, v.w, part[r][3]);
+            }
             idx[r] += bx ? stx[r] : sty[r];
             cx[r] += bx ? 1.f : 0.f;
             cy[r] += bx ? 0.f : 1.f;
@@ -145,18 +211,28 @@ __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
       // depend on how many rays share the warp's trip count
 #pragma unroll
       for (int r = 0; r < RPT; r++)
-        if (base < nseg[r]) kahan_add(acc[r], comp[r], part[r]);
+        if (base < nseg[r])
+#pragma unroll
+          for (int m = 0; m < G; m++) kahan_add(acc[r][m], comp[r][m], part[r][m]);
     }
     const int row0 = view * S.ndets;
 #pragma unroll
     for (int r = 0; r < RPT; r++) {
       const int det = det0 + r;
-      if (det < S.ndets) fp_epilogue(S, L, row0 + det, acc[r] - comp[r], s0);
+      if (det < S.ndets)
+#pragma unroll
+        for (int m = 0; m < G; m++)
+          if (act[m]) fp_epilogue(*M[m], L, row0 + det, acc[r][m] - comp[r][m], s0[m]);
     }
   }
   if (stage_reduces(L.stage)) {
-    double v[1] = {s0};
-    reduce_and_finalize<1>(S, L, v, local_cta, ncta);
+#pragma unroll
+    for (int m = 0; m < G; m++) {
+      if (!act[m]) continue;
+      double v[1] = {s0[m]};
+      reduce_and_finalize<1>(*M[m], L, v, local_cta, ncta);
+      __syncthreads();  // the shared scratch of the reduction is reused by the next member
+    }
   }
 }
 
@@ -175,15 +251,16 @@ __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
 // sum.  A tile's view blocks may be split over several CTAs (load balance when
 // a launch has few tiles); their 64-bit sums add exactly in global memory.  Integer addition is associative, so the result does not depend on the
 // order in which lanes, warps or views arrive (deterministic, no float
-// atomics).
+// atomics).  Scans of a batch that share the plan are back-projected together
+// (up to kGroupMax, listed in the lead scan): each run is loaded and walked
+// once and its weights go to every member's accumulator, each with the
+// member's own residual and scale, so each member's integer sum is exactly the
+// one it gets alone.
 constexpr int kBpPitch = kBpTile + 1;  // padded row pitch of the accumulator
-// accumulator copies, chosen by lane (1, 4 and 8 copies measure alike on the
-// C2 back projection, 2 copies about 8 % slower)
-constexpr int kBpCopies = 1;
 constexpr int kBpAccWords = kBpTile * kBpPitch;
-// copies start 32/kBpCopies banks apart, so the same pixel in different copies
-// falls in different banks
-constexpr int kBpCopyStride = kBpAccWords + ((32 / kBpCopies - kBpAccWords % 32) % 32 + 32) % 32;
+// members' accumulators start 32/kGroupMax banks apart, so the same pixel of
+// different members falls in different banks
+constexpr int kBpMemStride = kBpAccWords + ((32 / kGroupMax - kBpAccWords % 32) % 32 + 32) % 32;
 
 // max |r| of each scan's input sinogram, in kBpMaxParts partial maxima
 __global__ void __launch_bounds__(256) sino_absmax_kernel(const Launch L) {
@@ -205,10 +282,21 @@ __global__ void __launch_bounds__(256) sino_absmax_kernel(const Launch L) {
   }
 }
 
-__global__ void __launch_bounds__(256) fan_bp_kernel(const Launch L) {
+template <int G>
+__device__ __forceinline__ void fan_bp_body(const Launch &L) {
   const int scan = L.scans ? find_scan(L.prefix, L.nscans, blockIdx.x) : 0;
   const ScanDev &S = scan_of(L, scan);
-  if (!flow_active(S, L.flow)) return;
+  const int nm = L.scans ? S.nmem : 1;
+  const ScanDev *M[G];
+  bool act[G];
+  bool any = false;
+#pragma unroll
+  for (int m = 0; m < G; m++) {
+    M[m] = L.scans ? &L.scans[S.mem[m < nm ? m : 0]] : &L.single;
+    act[m] = m < nm && flow_active(*M[m], L.flow);
+    any |= act[m];
+  }
+  if (!any) return;
   const int cta0 = L.scans ? __ldg(L.prefix + scan) : 0;
   const int ncta = L.scans ? __ldg(L.prefix + scan + 1) - cta0 : gridDim.x;
   const int local_cta = blockIdx.x - cta0;
@@ -218,36 +306,50 @@ __global__ void __launch_bounds__(256) fan_bp_kernel(const Launch L) {
   const int vb0 = split * S.nvb / S.bp_split, vb1 = (split + 1) * S.nvb / S.bp_split;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const bool real = split < S.bp_split;
-  __shared__ int acc[kBpCopies * kBpCopyStride];
-  __shared__ float wmax[8];
+  __shared__ int acc[G * kBpMemStride];
+  __shared__ float wmax[G][8];
   __shared__ int last_split;
-  for (int i = threadIdx.x; i < kBpCopies * kBpCopyStride; i += blockDim.x) acc[i] = 0;
-  int *const my_acc = acc + (lane % kBpCopies) * kBpCopyStride;
-  const float *__restrict__ sino = S.buf[L.in_buf];
+  for (int i = threadIdx.x; i < G * kBpMemStride; i += blockDim.x) acc[i] = 0;
+  const float *__restrict__ sino[G];
   const int32_t *toff = S.tile_off + (size_t)(real ? tile : 0) * S.nvb;
-  // fixed-point scale from the largest |r| of the scan (the same in every
-  // split of a tile, so split sums add exactly)
-  float m = threadIdx.x < kBpMaxParts ? S.bpmax[threadIdx.x] : 0.f;
+  // fixed-point scale from the largest |r| of each member's sinogram (the same
+  // in every split of a tile, so split sums add exactly)
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if (lane == 0) wmax[warp] = m;
+  for (int m = 0; m < G; m++) {
+    sino[m] = M[m]->buf[L.in_buf];
+    float mx = (act[m] && threadIdx.x < kBpMaxParts) ? M[m]->bpmax[threadIdx.x] : 0.f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (lane == 0) wmax[m][warp] = mx;
+  }
   __syncthreads();
-  m = wmax[0];
-  for (int w = 1; w < (int)(blockDim.x >> 5); w++) m = fmaxf(m, wmax[w]);
-  // every |w r| <= 1.5 * pixel * m < 2^ex; terms are scaled below 2^bp_term_bits,
-  // so one view block's terms fit a 32-bit accumulator without overflow
-  int ex = 0;
-  frexpf(fmaxf(1.5f * S.pixel_mm * m, 1e-30f), &ex);
-  const int sexp = min(S.bp_term_bits - ex, 120);
-  const float scale = ldexpf(1.f, sexp);
+  int sexp[G];
+  float scale[G];
+  bool use[G];
+  bool any_use = false;
+#pragma unroll
+  for (int m = 0; m < G; m++) {
+    float mx = wmax[m][0];
+    for (int w = 1; w < (int)(blockDim.x >> 5); w++) mx = fmaxf(mx, wmax[m][w]);
+    // every |w r| <= 1.5 * pixel * max|r| < 2^ex; terms are scaled below
+    // 2^bp_term_bits, so one view block's terms fit a 32-bit accumulator
+    int ex = 0;
+    frexpf(fmaxf(1.5f * S.pixel_mm * mx, 1e-30f), &ex);
+    sexp[m] = min(S.bp_term_bits - ex, 120);
+    scale[m] = ldexpf(1.f, sexp[m]);
+    use[m] = real && act[m] && mx > 0.f;
+    any_use |= use[m];
+  }
   const int own = (threadIdx.x >> 4) * kBpPitch + (threadIdx.x & 15);  // this thread's pixel
-  long long total = 0;  // exact sum over view blocks
+  long long total[G];  // exact sums over view blocks
+#pragma unroll
+  for (int m = 0; m < G; m++) total[m] = 0;
   // w*r*scale + 1.5*2^23 rounds w*r*scale to an integer in the float's low
   // mantissa bits (|w*r*scale| < 2^22), so one FFMA does the scaling and the
   // round-to-nearest conversion
   constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
   constexpr int kMagicBits = 0x4B400000;
-  if (real && m > 0.f) {
+  if (any_use) {
     for (int vb = vb0; vb < vb1; vb++) {
       const int b0 = __ldg(toff + vb), b1 = __ldg(toff + vb + 1);
       // two-stage pipeline: the next chunk's dependent loads fly during this walk
@@ -255,20 +357,25 @@ __global__ void __launch_bounds__(256) fan_bp_kernel(const Launch L) {
       int c = b0 + warp * 32;
       uint4 e = (c + lane < b1) ? __ldg(S.run + c + lane) : kZ;
       uint4 h1 = __ldg(reinterpret_cast<const uint4 *>(S.rays + e.x) + 1);
-      float r0 = __ldg(sino + e.x);
+      float r0[G];
+#pragma unroll
+      for (int m = 0; m < G; m++) r0[m] = use[m] ? __ldg(sino[m] + e.x) : 0.f;
       for (; c < b1; c += blockDim.x) {
         const int cn = c + blockDim.x;
         const uint4 en = (cn + lane < b1) ? __ldg(S.run + cn + lane) : kZ;
         const uint4 h1n = __ldg(reinterpret_cast<const uint4 *>(S.rays + en.x) + 1);
-        const float rn = __ldg(sino + en.x);
+        float rn[G], rs[G];
+#pragma unroll
+        for (int m = 0; m < G; m++) {
+          rn[m] = use[m] ? __ldg(sino[m] + en.x) : 0.f;
+          rs[m] = r0[m] * scale[m];
+        }
         const bool valid = c + lane < b1;
-        const float rv = r0;
         const int k_in = (int)(e.y & 0x3fffu), nk = valid ? (int)((e.y >> 14) & 31u) : 0;
         const int cx_in = (int)(e.y >> 19);
         const float ax = __uint_as_float(h1.x), ay = __uint_as_float(h1.y);
         const float lx = __uint_as_float(h1.z), ly = __uint_as_float(h1.w);
         uint32_t wnd = e.z;  // the run's decision bits
-        const float rs = rv * scale;
         float cxf = (float)cx_in, cyf = (float)(k_in - cx_in);
         float prev = 0.f;
         if (k_in > 0) prev = (e.w & 1024u) ? fmaf(cxf - 1.f, lx, ax) : fmaf(cyf - 1.f, ly, ay);
@@ -287,7 +394,9 @@ __global__ void __launch_bounds__(256) fan_bp_kernel(const Launch L) {
           const float cur = bx ? nx : ny;
           const float wt = cur - prev;
           prev = cur;
-          atomicAdd(&my_acc[sidx], __float_as_int(fmaf(wt, rs, kMagic)) - kMagicBits);
+#pragma unroll
+          for (int m = 0; m < G; m++)
+            if (use[m]) atomicAdd(&acc[m * kBpMemStride + sidx], __float_as_int(fmaf(wt, rs[m], kMagic)) - kMagicBits);
           sidx += bx ? dsx : dsy;
           cxf += bx ? 1.f : 0.f;
           cyf += bx ? 0.f : 1.f;
@@ -300,20 +409,24 @@ __global__ void __launch_bounds__(256) fan_bp_kernel(const Launch L) {
           const float cur = bx ? nx : ny;
           const float wt = cur - prev;
           prev = cur;
-          if (t < nk) atomicAdd(&my_acc[sidx], __float_as_int(fmaf(wt, rs, kMagic)) - kMagicBits);
+          if (t < nk)
+#pragma unroll
+            for (int m = 0; m < G; m++)
+              if (use[m]) atomicAdd(&acc[m * kBpMemStride + sidx], __float_as_int(fmaf(wt, rs[m], kMagic)) - kMagicBits);
           sidx += bx ? dsx : dsy;
           cxf += bx ? 1.f : 0.f;
           cyf += bx ? 0.f : 1.f;
         }
         e = en;
         h1 = h1n;
-        r0 = rn;
+#pragma unroll
+        for (int m = 0; m < G; m++) r0[m] = rn[m];
       }
       __syncthreads();
 #pragma unroll
-      for (int cpy = 0; cpy < kBpCopies; cpy++) {
-        total += acc[cpy * kBpCopyStride + own];
-        acc[cpy * kBpCopyStride + own] = 0;
+      for (int m = 0; m < G; m++) {
+        total[m] += acc[m * kBpMemStride + own];
+        acc[m * kBpMemStride + own] = 0;
       }
       __syncthreads();
     }
@@ -323,10 +436,13 @@ __global__ void __launch_bounds__(256) fan_bp_kernel(const Launch L) {
   const bool mine = real && x < S.n && y < S.n;
   bool finish = real;
   if (S.bp_split > 1) {
-    // exact integer sums meet in the scan's 64-bit accumulator; the tile's
-    // last split to arrive takes the total (and leaves zeros) and finishes
-    unsigned long long *gacc = S.bp_acc + (size_t)x * S.n + y;
-    if (mine && total != 0) atomicAdd(gacc, (unsigned long long)total);
+    // exact integer sums meet in each member's 64-bit accumulator; the tile's
+    // last split to arrive (one ticket for the group) takes the totals, leaves
+    // zeros and finishes
+#pragma unroll
+    for (int m = 0; m < G; m++)
+      if (act[m] && mine && total[m] != 0)
+        atomicAdd(M[m]->bp_acc + (size_t)x * S.n + y, (unsigned long long)total[m]);
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) last_split = real && atomicAdd(&S.bp_cnt[tile], 1) == S.bp_split - 1;
@@ -334,20 +450,31 @@ __global__ void __launch_bounds__(256) fan_bp_kernel(const Launch L) {
     finish = last_split;
     if (finish) {
       __threadfence();
-      total = mine ? (long long)atomicExch(gacc, 0ull) : 0;
+#pragma unroll
+      for (int m = 0; m < G; m++)
+        total[m] = (act[m] && mine) ? (long long)atomicExch(M[m]->bp_acc + (size_t)x * S.n + y, 0ull) : 0;
       if (threadIdx.x == 0) S.bp_cnt[tile] = 0;
     }
   }
-  double s0 = 0.0;
-  if (finish && mine) {
-    const float val = (float)((double)total * ldexp(1.0, -sexp));
-    bp_epilogue(S, L, 0, x, y, val, s0);
-  }
-  if (stage_reduces(L.stage)) {
-    double v[1] = {s0};
-    reduce_and_finalize<1>(S, L, v, local_cta, ncta);
+#pragma unroll
+  for (int m = 0; m < G; m++) {
+    if (!act[m]) continue;
+    double s0 = 0.0;
+    if (finish && mine) {
+      const float val = (float)((double)total[m] * ldexp(1.0, -sexp[m]));
+      bp_epilogue(*M[m], L, 0, x, y, val, s0);
+    }
+    if (stage_reduces(L.stage)) {
+      double v[1] = {s0};
+      reduce_and_finalize<1>(*M[m], L, v, local_cta, ncta);
+      __syncthreads();  // the shared scratch of the reduction is reused by the next member
+    }
   }
 }
+
+__global__ void __launch_bounds__(256) fan_bp_kernel(const Launch L) { fan_bp_body<1>(L); }
+// the member arrays need registers: at most 128 per thread, two CTAs per SM
+__global__ void __launch_bounds__(256, 2) fan_bp_group_kernel(const Launch L) { fan_bp_body<kGroupMax>(L); }
 
 // ---------------------------------------------------------------------------
 // GoldenC parallel beam
@@ -520,12 +647,21 @@ cudaError_t launch_fp(const Launch &L, int kind, int rpt, int nctas, cudaStream_
   } else if (kind == AT_GEOM_CONE) {
     return launch_cone_fp(L, nctas, st);
   } else if (rpt == 4) {
-    fan_fp_kernel<4><<<nctas, 128, 0, st>>>(L);
+    fan_fp_kernel<4, 1><<<nctas, 128, 0, st>>>(L);
   } else if (rpt == 2) {
-    fan_fp_kernel<2><<<nctas, 128, 0, st>>>(L);
+    fan_fp_kernel<2, 1><<<nctas, 128, 0, st>>>(L);
   } else {
-    fan_fp_kernel<1><<<nctas, 128, 0, st>>>(L);
+    fan_fp_kernel<1, 1><<<nctas, 128, 0, st>>>(L);
   }
+  return cudaGetLastError();
+}
+
+// Forward projection of a batch whose scans sharing a plan are grouped: the
+// members' inputs are interleaved (over the pixel-pass CTAs of Lpix), then
+// each group's rays are walked once, one ray per thread.
+cudaError_t launch_fp_group(const Launch &L, const Launch &Lpix, int nctas, int pix_nctas, cudaStream_t st) {
+  fp_pack_kernel<<<pix_nctas, 256, 0, st>>>(Lpix);
+  fan_fp_kernel<1, kGroupMax><<<nctas, 128, 0, st>>>(L);
   return cudaGetLastError();
 }
 
@@ -540,7 +676,10 @@ cudaError_t launch_bp(const Launch &L, int kind, int nctas, cudaStream_t st, con
     return launch_cone_bp(L, nctas, *Lpix, pix_nctas, st);
   } else {
     sino_absmax_kernel<<<(L.scans ? L.nscans : 1) * kBpMaxParts, 256, 0, st>>>(L);
-    fan_bp_kernel<<<nctas, 256, 0, st>>>(L);
+    if (L.group > 1)  // scans sharing a plan walk its runs once
+      fan_bp_group_kernel<<<nctas, 256, 0, st>>>(L);
+    else
+      fan_bp_kernel<<<nctas, 256, 0, st>>>(L);
   }
   return cudaGetLastError();
 }

@@ -20,6 +20,7 @@ int fp_ctas(const ScanDev &S, int rpt);
 int bp_ctas(const ScanDev &S);
 int pix_ctas(const ScanDev &S);
 cudaError_t launch_fp(const Launch &L, int kind, int rpt, int nctas, cudaStream_t st);
+cudaError_t launch_fp_group(const Launch &L, const Launch &Lpix, int nctas, int pix_nctas, cudaStream_t st);
 cudaError_t launch_bp(const Launch &L, int kind, int nctas, cudaStream_t st, const Launch *Lpix, int pix_nctas);
 cudaError_t launch_pixel(int which, const Launch &L, int nctas, cudaStream_t st);
 cudaError_t launch_flags(const ScanDev *scans, int nscans, int mode, cudaStream_t st);
@@ -67,7 +68,7 @@ enum Family { FAM_FP = 0, FAM_PIX = 1, FAM_SINO = 2, FAM_BP = 3 };
 size_t align_up(size_t x) { return (x + 255) & ~size_t(255); }
 
 struct ScanLayout {
-  size_t img_bytes, sino_bytes, partial_bytes, trace_bytes, bp_bytes, total;
+  size_t img_bytes, sino_bytes, partial_bytes, trace_bytes, bp_bytes, pack_bytes, total;
 };
 
 ScanLayout layout_of(const Plan &p, int rpt) {
@@ -78,12 +79,17 @@ ScanLayout layout_of(const Plan &p, int rpt) {
   ScanDev tmp;
   fill_scan_plan(tmp, p);
   tmp.bp_split = kBpMaxSplit;  // size the partials for the largest split
-  const int maxcta = std::max({fp_ctas(tmp, rpt), bp_ctas(tmp), pix_ctas(tmp), (int)((nbins + 255) / 256)});
+  // and for one ray per thread (what grouped forward projections use)
+  const int maxcta = std::max({fp_ctas(tmp, rpt), fp_ctas(tmp, 1), bp_ctas(tmp), pix_ctas(tmp),
+                               (int)((nbins + 255) / 256)});
   L.partial_bytes = align_up((size_t)maxcta * 4 * sizeof(double));
   L.trace_bytes = align_up((size_t)kTraceCap * 10 * sizeof(double));
   L.bp_bytes = bp_scratch_bytes(p);
+  // fan beam and ray tables: a group's forward-projector inputs, interleaved
+  const bool packs = p.kind == AT_GEOM_FAN || p.kind == AT_GEOM_RAYS;
+  L.pack_bytes = packs ? align_up(sizeof(float4) * (size_t)p.n * p.n) : 0;
   L.total = L.img_bytes * B_NIMG + L.sino_bytes * (B_NBUF - B_NIMG) + L.partial_bytes + L.trace_bytes +
-            L.bp_bytes + align_up(sizeof(Ctl));
+            L.bp_bytes + L.pack_bytes + align_up(sizeof(Ctl));
   return L;
 }
 }  // namespace
@@ -107,6 +113,8 @@ void carve_scan(ScanDev &S, const Plan &p, int rpt, char *cur) {
   cur += lay.trace_bytes;
   carve_bp_scratch(S, p, cur);
   cur += lay.bp_bytes;
+  S.pack = lay.pack_bytes ? (float4 *)cur : nullptr;
+  cur += lay.pack_bytes;
   S.ctl = (Ctl *)cur;
 }
 
@@ -160,24 +168,43 @@ int Batch::set(const ScanDev *scans, int n, int kind_, int rpt_, cudaStream_t st
     AT_CUDA_TRY(cudaMalloc(&prefix_d, sizeof(int) * 4 * (cap + 1)));
   }
   nscans = n;
-  // back-projection split from the tiles of the whole launch
   std::vector<ScanDev> sc(scans, scans + n);
+  // scans sharing a plan (fan beam, ray tables) are projected together, up to
+  // kGroupMax per group: the lead (first of them) lists the members and gets
+  // the projector CTAs, the others none
+  group = 1;
+  for (int s = 0; s < n; s++) {
+    sc[s].nmem = 1;
+    sc[s].mem[0] = s;
+  }
   if (kind == AT_GEOM_FAN || kind == AT_GEOM_RAYS) {
+    for (int s = 1; s < n; s++) {
+      for (int t = 0; t < s; t++) {
+        if (sc[t].nmem > 0 && sc[t].nmem < kGroupMax && sc[t].rays == sc[s].rays) {
+          sc[t].mem[sc[t].nmem++] = s;
+          sc[s].nmem = 0;
+          break;
+        }
+      }
+    }
+    // back-projection split from the tiles of the whole launch
     int tiles = 0, nvb = 1 << 30;
     for (const auto &S : sc) {
-      tiles += S.ntiles_y * S.ntiles_y;
+      group = std::max(group, S.nmem);
+      if (S.nmem) tiles += S.ntiles_y * S.ntiles_y;
       nvb = std::min(nvb, S.nvb);
     }
     const int split = bp_split_for(tiles, nvb);
     for (auto &S : sc) S.bp_split = split;
   }
+  const int frpt = group > 1 ? 1 : rpt;  // the grouped forward projector walks one ray per thread
   scans = sc.data();
   std::vector<int> pref(4 * (n + 1), 0);
   for (int s = 0; s < n; s++) {
-    pref[FAM_FP * (n + 1) + s + 1] = pref[FAM_FP * (n + 1) + s] + fp_ctas(scans[s], rpt);
+    pref[FAM_FP * (n + 1) + s + 1] = pref[FAM_FP * (n + 1) + s] + (scans[s].nmem ? fp_ctas(scans[s], frpt) : 0);
     pref[FAM_PIX * (n + 1) + s + 1] = pref[FAM_PIX * (n + 1) + s] + pix_ctas(scans[s]);
     pref[FAM_SINO * (n + 1) + s + 1] = pref[FAM_SINO * (n + 1) + s] + (scans[s].nbins + 255) / 256;
-    pref[FAM_BP * (n + 1) + s + 1] = pref[FAM_BP * (n + 1) + s] + bp_ctas(scans[s]);
+    pref[FAM_BP * (n + 1) + s + 1] = pref[FAM_BP * (n + 1) + s] + (scans[s].nmem ? bp_ctas(scans[s]) : 0);
   }
   fp_total = pref[FAM_FP * (n + 1) + n];
   pix_total = pref[FAM_PIX * (n + 1) + n];
@@ -196,6 +223,7 @@ Launch Batch::base_launch(int family) const {
   L.nscans = nscans;
   L.prefix = prefix_d + family * (nscans + 1);
   L.aux_buf = -1;
+  L.group = (family == FAM_FP || family == FAM_BP) ? group : 1;
   return L;
 }
 
@@ -226,8 +254,15 @@ int Batch::enqueue_image(cudaStream_t st) {
     L.in_buf = in;
     L.aux_buf = aux;
     L.k = k;
-    AT_CUDA_TRY(launch_fp(L, kind, rpt, fp_total, st));
-    launches++;
+    if (group > 1) {  // interleave each group's inputs, then one walk per group
+      Launch Lp = L;
+      Lp.prefix = prefix_d + FAM_PIX * (nscans + 1);
+      AT_CUDA_TRY(launch_fp_group(L, Lp, fp_total, pix_total, st));
+      launches += 2;
+    } else {
+      AT_CUDA_TRY(launch_fp(L, kind, rpt, fp_total, st));
+      launches++;
+    }
     return AT_OK;
   };
   auto bp = [&](int stage, int u, int k) -> int {

@@ -30,6 +30,7 @@ struct Batch {
   ScanDev *scans_d = nullptr;
   int *prefix_d = nullptr;  // [4][cap+1]: forward-projector, pixel-pass, sinogram-pass, back-projector CTAs
   int fp_total = 0, pix_total = 0, sino_total = 0, bp_total = 0;
+  int group = 1;            // largest group of scans sharing a plan (projected together)
   int launches = 0;         // kernel launches of the last enqueue_outer
   Batch() = default;
   Batch(const Batch &) = delete;

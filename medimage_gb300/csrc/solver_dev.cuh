@@ -75,6 +75,7 @@ struct Ctl {
 constexpr int kTraceCap = 4096;  // records per scan (10 doubles each)
 constexpr int kBpMaxParts = 64;  // CTAs of the max |r| pass per scan
 constexpr int kBpMaxSplit = 8;   // most CTAs one back-projection tile is split over
+constexpr int kGroupMax = 4;     // most scans of one plan whose projections share a walk
 
 struct ScanDev {
   int kind, n, nviews, ndets;
@@ -105,6 +106,12 @@ struct ScanDev {
   unsigned long long *bp_acc;  // [npix]
   int *bp_cnt;                 // [ntiles]
   int bp_split;                // CTAs per tile (>= 1)
+  float4 *pack;                // [n*n] fan/ray plans: the group's forward-projector inputs, interleaved
+  // scans of a batch that share this scan's plan and are projected together
+  // with it: nmem members (scan indices, this one first) on the lead; 0 on
+  // the others, which get no projector CTAs of their own
+  int nmem;
+  int mem[kGroupMax];
   // state
   float *buf[B_NBUF];
   Ctl *ctl;
@@ -123,6 +130,7 @@ struct Launch {
   int in_buf, out_buf, aux_buf;  // buffer ids (meaning depends on the kernel)
   int k;                         // inner iteration this launch belongs to
   int flag;                      // kernel-specific (median this iteration, first pass, ...)
+  int group;                     // projector launches: largest group of scans sharing a plan
 };
 
 __device__ __forceinline__ int find_scan(const int *prefix, int nscans, int cta) {

@@ -90,6 +90,35 @@ def test_batch_equals_alone(engine, oracle):
         assert rel_l2(fb, fa) <= 1e-6 and rel_l2(vb, va) <= 1e-6
 
 
+def test_shared_plan_groups_equal_alone(engine, oracle):
+    """Scans of one plan are projected together (up to four per walk); a fifth
+    scan of that plan starts a second group, and a scan of another plan sits
+    between them.  Each must still reconstruct as it does alone."""
+    gA, _, _ = make_case(engine, oracle, 96, 2.0, 120, 160, seed=51)
+    gB, _, sB = make_case(engine, oracle, 64, 3.0, 90, 128, seed=52)
+    pA, pB = engine.Plan.fan(gA), engine.Plan.fan(gB)
+    sinos = []
+    for s in range(5):
+        ph = engine.phantom.ellipse_phantom(96, seed=60 + s, n_random=3 + s)
+        clean = oracle.fan_A(oracle.fan_from_engine(gA), ph.astype(np.float64))
+        sinos.append(engine.phantom.poisson_sinogram(clean, 1e4 * (s + 1), 160 + s))
+    plans = [pA, pA, pB, pA, pA, pA]
+    data = [sinos[0], sinos[1], sB, sinos[2], sinos[3], sinos[4]]
+    prm = engine.Params(iter_alt=2)
+    B = engine.Solver(plans, prm)
+    for i, d in enumerate(data):
+        B.set_sino(i, d)
+    B.run()
+    for i, (p, d) in enumerate(zip(plans, data)):
+        A1 = engine.Solver([p], prm)
+        A1.set_sino(0, d)
+        A1.run()
+        fa, va = A1.get(0)
+        fb, vb = B.get(i)
+        assert rel_l2(fb, fa) <= 1e-6 and rel_l2(vb, va) <= 1e-6, (i, rel_l2(fb, fa), rel_l2(vb, va))
+        assert exits(B.trace(i)) == exits(A1.trace(0))
+
+
 def test_reconstruct_host_matches_solver(engine, oracle):
     g, ph, sino = make_case(engine, oracle, 64, 3.0, 90, 128, seed=41)
     prm = engine.Params(iter_alt=2)

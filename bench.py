@@ -15,7 +15,11 @@ value  : slices/s with the sinograms resident in HBM, CUDA-event timed over K
 e2e    : the same through the C-ABI with host buffers: every step copies the
          sinograms in from pinned host memory and f, v back out.
 roofline: the dominant kernel timed alone with CUDA events on its stream, at
-         the same workload, against the measured HBM copy bandwidth.
+         the same workload, against the measured HBM copy bandwidth.  The
+         step's slices share a plan, so it runs the grouped projectors (one
+         walk of the plan for up to four slices); those are timed through a
+         projection set, their algorithmic bytes the sum over their slices (an
+         effective bandwidth: images and sinograms stay in L2).
 --impl reference: the reference algorithm on the host cores (the FP64 oracle
          restatement of GoldenC's solver with the fan tracer, all threads), each
          step one outer iteration of one slice, scaled to slices/s.
@@ -262,33 +266,52 @@ def run_ours(args):
                               "f_rel_l2_vs_exact": float(np.linalg.norm(fl - f0) / np.linalg.norm(f0))}
         lin.close()
 
-    # ---- roofline: the dominant kernel alone, same workload, CUDA events
-    d_img = torch.from_numpy(phantoms[0]).cuda()
-    d_sino = torch.from_numpy(sinos[0]).cuda()
-    d_out_s = torch.empty_like(d_sino)
-    d_out_i = torch.empty_like(d_img)
+    # ---- roofline: the dominant kernel alone, same workload, CUDA events.
+    # The step's slices share one plan, so its projections run grouped (up to
+    # four slices per walk of the plan): the grouped launches are timed through
+    # a projection set over the step's slices, the single-slice kernels beside
+    # them.  A grouped launch's algorithmic bytes are its slices' sum.
+    G = min(B, 4)
+    d_img = [torch.from_numpy(phantoms[b]).cuda() for b in range(G)]
+    d_sino = [torch.from_numpy(sinos[b]).cuda() for b in range(G)]
+    d_out_s = [torch.empty_like(t) for t in d_sino]
+    d_out_i = [torch.empty_like(t) for t in d_img]
+    pset = mg.ProjSet([plan] * G)
+    ptr = lambda ts: [t.data_ptr() for t in ts]  # noqa: E731
     kern = {}
-    for name, fn, nbytes in (
-            ("fan_fp_kernel", lambda: plan.forward_dev(d_img.data_ptr(), d_out_s.data_ptr(), st), 4 * S_seg + 4 * R),
-            ("fan_bp_kernel", lambda: plan.back_dev(d_sino.data_ptr(), d_out_i.data_ptr(), st), 4 * S_seg + 4 * P)):
+    cases = [
+        ("fan_fp_kernel", lambda: plan.forward_dev(d_img[0].data_ptr(), d_out_s[0].data_ptr(), st), 4 * S_seg + 4 * R),
+        ("fan_bp_kernel", lambda: plan.back_dev(d_sino[0].data_ptr(), d_out_i[0].data_ptr(), st), 4 * S_seg + 4 * P)]
+    if G > 1:
+        cases += [
+            ("fan_fp_kernel<group>", lambda: pset.forward_dev(ptr(d_img), ptr(d_out_s), st), G * (4 * S_seg + 4 * R)),
+            ("fan_bp_group_kernel", lambda: pset.back_dev(ptr(d_sino), ptr(d_out_i), st), G * (4 * S_seg + 4 * P))]
+    for name, fn, nbytes in cases:
         for _ in range(3):
             fn()
+        # L2 flushed before every timed launch (as in the step, where the back
+        # projector's run list evicts the forward projector's plan)
         reps = 20
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(tstream)
-        for _ in range(reps):
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+        for e0, e1 in evs:
+            with torch.cuda.stream(tstream):
+                flush.zero_()
+            e0.record(tstream)
             fn()
-        e1.record(tstream)
+            e1.record(tstream)
         torch.cuda.synchronize()
-        kern[name] = {"ms": e0.elapsed_time(e1) / reps, "bytes": nbytes}
+        kern[name] = {"ms": sum(e0.elapsed_time(e1) for e0, e1 in evs) / reps, "bytes": nbytes}
     # calls per slice in the timed workload
     K, KI = prm.iter_alt, prm.iter_image
     fp_calls = K * (3 * KI - 1) if prm.mode == 0 else None
     bp_calls = K * KI
     if fp_calls is None:
         fp_calls = K * (KI + 2)
-    share = {n: kern[n]["ms"] * (fp_calls if "fp" in n else bp_calls) for n in kern}
+    # the kernels the step runs: grouped when the step holds several slices
+    ran = [n for n in kern if ("group" in n) == (G > 1)]
+    share = {n: kern[n]["ms"] * (fp_calls if "fp" in n else bp_calls) for n in ran}
     dom = max(share, key=share.get)
+    pset.close()
     peak, peak_kind = measured_peak_hbm()
     achieved = kern[dom]["bytes"] / (kern[dom]["ms"] / 1e3) / 1e9
     traffic = profile_traffic(dom)

@@ -146,11 +146,27 @@ int at_plan_trace_ray(const at_plan *plan, int32_t view, int32_t det, int32_t *h
 /* ---- projectors (FP32, device buffers) ---- */
 /* d_sino[view][det] = sum over the ray's segments of d_img[pixel] * weight */
 int at_forward(const at_plan *plan, const float *d_img, float *d_sino, void *stream);
-/* d_img = A^T d_sino, a deterministic per-pixel gather (no atomics) */
+/* d_img = A^T d_sino; deterministic: each pixel is an exact integer sum of
+ * fixed-point terms (no float atomics), so the result does not depend on
+ * scheduling */
 int at_back(const at_plan *plan, const float *d_sino, float *d_img, void *stream);
 /* host-buffer forms: copy in, project, copy out, synchronise */
 int at_forward_host(const at_plan *plan, const float *h_img, float *h_sino);
 int at_back_host(const at_plan *plan, const float *h_sino, float *h_img);
+
+/* ---- projection sets: several images through their plans in one launch ----
+ * Batched form of at_forward / at_back (the reference projects one slice per
+ * call: origin/GoldenC/src/proj.h:6-7 A and AStar).  Images whose plans are
+ * the same plan object are projected together, up to four per walk of the
+ * plan, with results identical to at_forward / at_back on each image.  A set
+ * holds device scratch: calls on one set must not overlap on the GPU. */
+typedef struct at_projset at_projset;
+int at_projset_create(at_plan *const *plans, int32_t n, at_projset **out);
+void at_projset_destroy(at_projset *ps);
+/* d_img[i] -> d_sino[i] through plans[i], i < n */
+int at_projset_forward(at_projset *ps, const float *const *d_img, float *const *d_sino, void *stream);
+/* d_sino[i] -> d_img[i] */
+int at_projset_back(at_projset *ps, const float *const *d_sino, float *const *d_img, void *stream);
 
 /* ---- device memory helpers for callers without a CUDA runtime binding ---- */
 int at_dev_alloc(void **d_ptr, size_t bytes);

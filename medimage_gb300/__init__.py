@@ -18,6 +18,7 @@ from .engine import (  # noqa: F401
     RowActionParams,
     Params,
     Plan,
+    ProjSet,
     Server,
     Solver,
     device_info,
@@ -36,6 +37,7 @@ __all__ = [
     "RowActionParams",
     "Params",
     "Plan",
+    "ProjSet",
     "Server",
     "Solver",
     "configs",

@@ -380,6 +380,33 @@ AT_API int at_solver_create(at_plan *const *plans, int32_t nscans, const at_para
 
 AT_API void at_solver_destroy(at_solver *s) { delete s; }
 
+AT_API int at_projset_create(at_plan *const *plans, int32_t n, at_projset **out) {
+  AT_CHECK_ARG(plans && n > 0 && out, "at_projset_create: bad argument");
+  *out = nullptr;
+  std::vector<Plan *> v;
+  for (int i = 0; i < n; i++) {
+    AT_CHECK_ARG(plans[i], "at_projset_create: null plan");
+    v.push_back(&plans[i]->p);
+  }
+  auto P = std::make_unique<at_projset>();
+  int rc = P->p.create(v);
+  if (rc) return rc;
+  *out = P.release();
+  return AT_OK;
+}
+
+AT_API void at_projset_destroy(at_projset *ps) { delete ps; }
+
+AT_API int at_projset_forward(at_projset *ps, const float *const *d_img, float *const *d_sino, void *stream) {
+  AT_CHECK_ARG(ps && d_img && d_sino, "at_projset_forward: null argument");
+  return ps->p.project(true, d_img, d_sino, (cudaStream_t)stream);
+}
+
+AT_API int at_projset_back(at_projset *ps, const float *const *d_sino, float *const *d_img, void *stream) {
+  AT_CHECK_ARG(ps && d_sino && d_img, "at_projset_back: null argument");
+  return ps->p.project(false, d_sino, d_img, (cudaStream_t)stream);
+}
+
 #define AT_SCAN_ARG(s, scan) \
   AT_CHECK_ARG((s) && (scan) >= 0 && (scan) < (s)->s.nscans, "solver: scan index out of range")
 

@@ -129,8 +129,7 @@ __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
     // blocks holding a ray that leaves the grid take the checked path throughout
     const int wfull = __ldg(S.blk_off + blk) ? 0 : (int)(__reduce_min_sync(0xffffffffu, (unsigned)my_min) >> 5);
     const uint32_t *wp = S.bits + __ldg(S.blk_word + blk) + in_blk;
-    for (int w = 0; w < nwords; w++) {
-      uint32_t bw[RPT];
+    auto load_bits = [&](int w, uint32_t(&bw)[RPT]) {
       if constexpr (RPT == 4) {
         const uint4 t = __ldg(reinterpret_cast<const uint4 *>(wp + (size_t)w * kRayBlock));
         bw[0] = t.x;
@@ -144,6 +143,10 @@ __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
       } else {
         bw[0] = __ldg(wp + (size_t)w * kRayBlock);
       }
+    };
+    for (int w = 0; w < nwords; w++) {
+      uint32_t bw[RPT];
+      load_bits(w, bw);
       float part[RPT][G];
 #pragma unroll
       for (int r = 0; r < RPT; r++)
@@ -256,11 +259,18 @@ __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
 // once and its weights go to every member's accumulator, each with the
 // member's own residual and scale, so each member's integer sum is exactly the
 // one it gets alone.
+// Lanes of a warp that add to the same pixel in one instruction serialise, and
+// a warp's runs (similar lengths through one tile, from nearby views) often
+// meet: each member therefore keeps C accumulator copies, lane l adding to copy
+// l % C, with copies 32/C banks apart.
 constexpr int kBpPitch = kBpTile + 1;  // padded row pitch of the accumulator
 constexpr int kBpAccWords = kBpTile * kBpPitch;
-// members' accumulators start 32/kGroupMax banks apart, so the same pixel of
-// different members falls in different banks
-constexpr int kBpMemStride = kBpAccWords + ((32 / kGroupMax - kBpAccWords % 32) % 32 + 32) % 32;
+constexpr int kBpCopies1 = 4;  // copies, single-scan launches (C2: 1 copy 0.33 ms, 4 copies 0.275 ms)
+constexpr int kBpCopiesG = 4;  // copies per member, grouped launches
+template <int C>
+constexpr int bp_copy_stride() {
+  return kBpAccWords + ((32 / C - kBpAccWords % 32) % 32 + 32) % 32;
+}
 
 // max |r| of each scan's input sinogram, in kBpMaxParts partial maxima
 __global__ void __launch_bounds__(256) sino_absmax_kernel(const Launch L) {
@@ -282,8 +292,10 @@ __global__ void __launch_bounds__(256) sino_absmax_kernel(const Launch L) {
   }
 }
 
-template <int G>
+template <int G, int C>
 __device__ __forceinline__ void fan_bp_body(const Launch &L) {
+  constexpr int kStride = bp_copy_stride<C>();  // one copy
+  constexpr int kMemStride = C * kStride;       // one member
   const int scan = L.scans ? find_scan(L.prefix, L.nscans, blockIdx.x) : 0;
   const ScanDev &S = scan_of(L, scan);
   const int nm = L.scans ? S.nmem : 1;
@@ -306,10 +318,11 @@ __device__ __forceinline__ void fan_bp_body(const Launch &L) {
   const int vb0 = split * S.nvb / S.bp_split, vb1 = (split + 1) * S.nvb / S.bp_split;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const bool real = split < S.bp_split;
-  __shared__ int acc[G * kBpMemStride];
+  __shared__ int acc[G * kMemStride];
   __shared__ float wmax[G][8];
   __shared__ int last_split;
-  for (int i = threadIdx.x; i < G * kBpMemStride; i += blockDim.x) acc[i] = 0;
+  for (int i = threadIdx.x; i < G * kMemStride; i += blockDim.x) acc[i] = 0;
+  int *const my_acc = acc + (lane % C) * kStride;
   const float *__restrict__ sino[G];
   const int32_t *toff = S.tile_off + (size_t)(real ? tile : 0) * S.nvb;
   // fixed-point scale from the largest |r| of each member's sinogram (the same
@@ -396,7 +409,7 @@ __device__ __forceinline__ void fan_bp_body(const Launch &L) {
           prev = cur;
 #pragma unroll
           for (int m = 0; m < G; m++)
-            if (use[m]) atomicAdd(&acc[m * kBpMemStride + sidx], __float_as_int(fmaf(wt, rs[m], kMagic)) - kMagicBits);
+            if (use[m]) atomicAdd(&my_acc[m * kMemStride + sidx], __float_as_int(fmaf(wt, rs[m], kMagic)) - kMagicBits);
           sidx += bx ? dsx : dsy;
           cxf += bx ? 1.f : 0.f;
           cyf += bx ? 0.f : 1.f;
@@ -412,7 +425,7 @@ __device__ __forceinline__ void fan_bp_body(const Launch &L) {
           if (t < nk)
 #pragma unroll
             for (int m = 0; m < G; m++)
-              if (use[m]) atomicAdd(&acc[m * kBpMemStride + sidx], __float_as_int(fmaf(wt, rs[m], kMagic)) - kMagicBits);
+              if (use[m]) atomicAdd(&my_acc[m * kMemStride + sidx], __float_as_int(fmaf(wt, rs[m], kMagic)) - kMagicBits);
           sidx += bx ? dsx : dsy;
           cxf += bx ? 1.f : 0.f;
           cyf += bx ? 0.f : 1.f;
@@ -424,10 +437,12 @@ __device__ __forceinline__ void fan_bp_body(const Launch &L) {
       }
       __syncthreads();
 #pragma unroll
-      for (int m = 0; m < G; m++) {
-        total[m] += acc[m * kBpMemStride + own];
-        acc[m * kBpMemStride + own] = 0;
-      }
+      for (int m = 0; m < G; m++)
+#pragma unroll
+        for (int c = 0; c < C; c++) {
+          total[m] += acc[m * kMemStride + c * kStride + own];
+          acc[m * kMemStride + c * kStride + own] = 0;
+        }
       __syncthreads();
     }
   }
@@ -472,9 +487,11 @@ __device__ __forceinline__ void fan_bp_body(const Launch &L) {
   }
 }
 
-__global__ void __launch_bounds__(256) fan_bp_kernel(const Launch L) { fan_bp_body<1>(L); }
+__global__ void __launch_bounds__(256) fan_bp_kernel(const Launch L) { fan_bp_body<1, kBpCopies1>(L); }
 // the member arrays need registers: at most 128 per thread, two CTAs per SM
-__global__ void __launch_bounds__(256, 2) fan_bp_group_kernel(const Launch L) { fan_bp_body<kGroupMax>(L); }
+__global__ void __launch_bounds__(256, 2) fan_bp_group_kernel(const Launch L) {
+  fan_bp_body<kGroupMax, kBpCopiesG>(L);
+}
 
 // ---------------------------------------------------------------------------
 // GoldenC parallel beam

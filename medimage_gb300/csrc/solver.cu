@@ -63,7 +63,6 @@ void fill_scan_plan(ScanDev &S, const Plan &p) {
 
 namespace {
 enum PixKernel { PK_UPD = 0, PK_PP, PK_COMMIT, PK_EDGE_INIT, PK_EDGE_D, PK_EDGE_UPD, PK_SINO, PK_INIT };
-enum Family { FAM_FP = 0, FAM_PIX = 1, FAM_SINO = 2, FAM_BP = 3 };
 
 size_t align_up(size_t x) { return (x + 255) & ~size_t(255); }
 
@@ -227,6 +226,28 @@ Launch Batch::base_launch(int family) const {
   return L;
 }
 
+int Batch::enqueue_fp(const Launch &L, cudaStream_t st) {
+  if (group > 1) {  // interleave each group's inputs, then one walk per group
+    Launch Lp = L;
+    Lp.prefix = prefix_d + FAM_PIX * (nscans + 1);
+    AT_CUDA_TRY(launch_fp_group(L, Lp, fp_total, pix_total, st));
+    launches += 2;
+  } else {
+    AT_CUDA_TRY(launch_fp(L, kind, rpt, fp_total, st));
+    launches++;
+  }
+  return AT_OK;
+}
+
+int Batch::enqueue_bp(const Launch &L, cudaStream_t st) {
+  Launch Lp = L;  // the per-pixel finishing pass of the cone-beam back projector
+  Lp.prefix = prefix_d + FAM_PIX * (nscans + 1);
+  AT_CUDA_TRY(launch_bp(L, kind, bp_total, st, &Lp, pix_total));
+  // max |r| pass + back projection (+ per-pixel finish for the cone beam)
+  launches += kind == AT_GEOM_GOLDNC ? 1 : kind == AT_GEOM_CONE ? 3 : 2;
+  return AT_OK;
+}
+
 int Batch::enqueue_init(cudaStream_t st) {
   Launch L = base_launch(FAM_PIX);
   L.flow = FLOW_ENABLED;
@@ -254,16 +275,7 @@ int Batch::enqueue_image(cudaStream_t st) {
     L.in_buf = in;
     L.aux_buf = aux;
     L.k = k;
-    if (group > 1) {  // interleave each group's inputs, then one walk per group
-      Launch Lp = L;
-      Lp.prefix = prefix_d + FAM_PIX * (nscans + 1);
-      AT_CUDA_TRY(launch_fp_group(L, Lp, fp_total, pix_total, st));
-      launches += 2;
-    } else {
-      AT_CUDA_TRY(launch_fp(L, kind, rpt, fp_total, st));
-      launches++;
-    }
-    return AT_OK;
+    return enqueue_fp(L, st);
   };
   auto bp = [&](int stage, int u, int k) -> int {
     Launch L = base_launch(FAM_BP);
@@ -273,12 +285,7 @@ int Batch::enqueue_image(cudaStream_t st) {
     L.out_buf = B_D;
     L.aux_buf = u;
     L.k = k;
-    Launch Lp = L;  // the per-pixel finishing pass of the cone-beam back projector
-    Lp.prefix = prefix_d + FAM_PIX * (nscans + 1);
-    AT_CUDA_TRY(launch_bp(L, kind, bp_total, st, &Lp, pix_total));
-    // max |r| pass + back projection (+ per-pixel finish for the cone beam)
-    launches += kind == AT_GEOM_GOLDNC ? 1 : kind == AT_GEOM_CONE ? 3 : 2;
-    return AT_OK;
+    return enqueue_bp(L, st);
   };
   auto pix = [&](int which, int flow, int stage, int in, int out, int aux, int k, int flag) -> int {
     Launch L = base_launch(which == PK_SINO ? FAM_SINO : FAM_PIX);
@@ -396,6 +403,68 @@ int Solver::create(const std::vector<Plan *> &pl, const at_params &prm) {
   AT_CUDA_TRY(cudaStreamSynchronize(own_stream));
   return AT_OK;
 }
+
+// ---------------------------------------------------------------- ProjSet
+int ProjSet::create(const std::vector<Plan *> &pl) {
+  if (pl.empty()) return set_error(AT_EINVAL, "projection set: no plans");
+  kind = pl[0]->kind;
+  auto family = [](int k) { return k == AT_GEOM_RAYS ? AT_GEOM_FAN : k; };
+  for (auto *p : pl)
+    if (family(p->kind) != family(kind))
+      return set_error(AT_EINVAL, "projection set: GoldenC, fan-beam/ray-table or cone-beam plans, not a mix");
+  plans = pl;
+  rpt = Solver::choose_rpt(pl);
+  const int n = (int)pl.size();
+  auto pack_of = [](const Plan &p) {
+    return (p.kind == AT_GEOM_FAN || p.kind == AT_GEOM_RAYS) ? align_up(sizeof(float4) * (size_t)p.n * p.n) : 0;
+  };
+  size_t total = 256;
+  for (auto *p : pl) total += bp_scratch_bytes(*p) + pack_of(*p);
+  if (cudaMalloc(&scratch, total) != cudaSuccess) {
+    cudaGetLastError();
+    return set_error(AT_ENOMEM, "projection set: device allocation of " + std::to_string(total) + " bytes failed");
+  }
+  AT_CUDA_TRY(cudaMemset(scratch, 0, total));
+  host.resize(n);
+  bound.assign(2 * n, nullptr);
+  char *cur = (char *)scratch;
+  for (int s = 0; s < n; s++) {
+    fill_scan_plan(host[s], *pl[s]);
+    carve_bp_scratch(host[s], *pl[s], cur);
+    cur += bp_scratch_bytes(*pl[s]);
+    host[s].pack = pack_of(*pl[s]) ? (float4 *)cur : nullptr;
+    cur += pack_of(*pl[s]);
+  }
+  return AT_OK;
+}
+
+int ProjSet::project(bool forward, const float *const *in, float *const *out, cudaStream_t st) {
+  const int n = (int)plans.size();
+  bool same = true;
+  for (int s = 0; s < n; s++) {
+    if (!in[s] || !out[s]) return set_error(AT_EINVAL, "projection set: null buffer");
+    same &= bound[2 * s] == in[s] && bound[2 * s + 1] == out[s];
+    host[s].buf[0] = const_cast<float *>(in[s]);
+    host[s].buf[1] = out[s];
+  }
+  if (!same) {  // re-point the device copy (and the CTA tables) at the new buffers
+    int rc = batch.set(host.data(), n, kind, rpt, st);
+    if (rc) return rc;
+    for (int s = 0; s < n; s++) {
+      bound[2 * s] = in[s];
+      bound[2 * s + 1] = out[s];
+    }
+  }
+  Launch L = batch.base_launch(forward ? FAM_FP : FAM_BP);
+  L.flow = FLOW_ALWAYS;
+  L.stage = ST_NONE;
+  L.in_buf = 0;
+  L.out_buf = 1;
+  L.aux_buf = -1;
+  return forward ? batch.enqueue_fp(L, st) : batch.enqueue_bp(L, st);
+}
+
+ProjSet::~ProjSet() { cudaFree(scratch); }
 
 Solver::~Solver() {
   if (graph_exec) cudaGraphExecDestroy(graph_exec);

@@ -22,6 +22,9 @@ void carve_bp_scratch(ScanDev &S, const Plan &p, char *mem);
 // CTAs per back-projection tile for a launch over `tiles` tiles
 int bp_split_for(int tiles, int nvb);
 
+// CTA-range families of a batch's launches (rows of Batch::prefix_d)
+enum Family { FAM_FP = 0, FAM_PIX = 1, FAM_SINO = 2, FAM_BP = 3 };
+
 // The launch sequence of the AT iteration over a set of scans: one launch per
 // kernel for the whole set, per-scan CTA ranges from prefix tables.
 struct Batch {
@@ -38,6 +41,10 @@ struct Batch {
   ~Batch();
   int set(const ScanDev *scans, int n, int kind, int rpt, cudaStream_t st);
   Launch base_launch(int family) const;
+  // one forward / back projection of every scan (L from base_launch(FAM_FP /
+  // FAM_BP) with flow, stage and buffers set); scans sharing a plan are grouped
+  int enqueue_fp(const Launch &L, cudaStream_t st);
+  int enqueue_bp(const Launch &L, cudaStream_t st);
   int enqueue_init(cudaStream_t st);
   int enqueue_outer(cudaStream_t st);
   int enqueue_image(cudaStream_t st);
@@ -76,7 +83,27 @@ struct Solver {
   int run(cudaStream_t st);
 };
 
+// A fixed list of plans projected together (at_projset_*): each call is one
+// launch per kernel for the whole list, scans sharing a plan grouped.  Holds
+// the scans' projector scratch (back-projection sums, interleaved group
+// inputs) in one allocation, so calls on one set must not overlap.
+struct ProjSet {
+  std::vector<Plan *> plans;
+  std::vector<ScanDev> host;
+  std::vector<const void *> bound;  // buffers the device copy of `host` points at
+  Batch batch;
+  void *scratch = nullptr;
+  int kind = AT_GEOM_FAN, rpt = 1;
+  int create(const std::vector<Plan *> &plans);
+  int project(bool forward, const float *const *in, float *const *out, cudaStream_t st);
+  ~ProjSet();
+};
+
 }  // namespace at
+
+struct at_projset {
+  at::ProjSet p;
+};
 
 struct at_solver {
   at::Solver s;

@@ -140,6 +140,10 @@ SIGNATURES = {
     "at_stream_sync": ([C.c_void_p], C.c_int),
     "at_solver_create": ([C.POINTER(C.c_void_p), C.c_int32, C.POINTER(_Params), C.POINTER(C.c_void_p)], C.c_int),
     "at_solver_destroy": ([C.c_void_p], None),
+    "at_projset_create": ([C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_void_p)], C.c_int),
+    "at_projset_destroy": ([C.c_void_p], None),
+    "at_projset_forward": ([C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.c_void_p], C.c_int),
+    "at_projset_back": ([C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.c_void_p], C.c_int),
     "at_solver_footprint": ([C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_size_t)], C.c_int),
     "at_solver_set_sino": ([C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p], C.c_int),
     "at_solver_set_sino_host": ([C.c_void_p, C.c_int32, _fp, C.c_void_p], C.c_int),
@@ -441,6 +445,41 @@ class Plan:
 def _plan_array(plans):
     arr = (C.c_void_p * len(plans))(*[p.handle for p in plans])
     return arr
+
+
+class ProjSet:
+    """Several images through their plans in one launch per kernel
+    (at_projset_*); images of the same Plan object are projected together, up
+    to four per walk of the plan.  Device pointers in, device pointers out."""
+
+    def __init__(self, plans):
+        self.plans = list(plans)
+        self._h = C.c_void_p()
+        _check("at_projset_create", lib().at_projset_create(_plan_array(self.plans), len(self.plans),
+                                                            C.byref(self._h)))
+
+    def close(self):
+        if self._h:
+            lib().at_projset_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ptrs(self, ptrs):
+        assert len(ptrs) == len(self.plans)
+        return (C.c_void_p * len(ptrs))(*[C.c_void_p(p) for p in ptrs])
+
+    def forward_dev(self, d_imgs, d_sinos, stream: int = 0) -> None:
+        _check("at_projset_forward", lib().at_projset_forward(self._h, self._ptrs(d_imgs), self._ptrs(d_sinos),
+                                                              C.c_void_p(stream)))
+
+    def back_dev(self, d_sinos, d_imgs, stream: int = 0) -> None:
+        _check("at_projset_back", lib().at_projset_back(self._h, self._ptrs(d_sinos), self._ptrs(d_imgs),
+                                                        C.c_void_p(stream)))
 
 
 class Solver:

@@ -229,12 +229,13 @@ __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
     }
   }
   if (stage_reduces(L.stage)) {
+    if constexpr (G == 1) {
+      reduce_and_finalize<1>(*M[0], L, s0, local_cta, ncta);
+    } else {
+      unsigned mask = 0;
 #pragma unroll
-    for (int m = 0; m < G; m++) {
-      if (!act[m]) continue;
-      double v[1] = {s0[m]};
-      reduce_and_finalize<1>(*M[m], L, v, local_cta, ncta);
-      __syncthreads();  // the shared scratch of the reduction is reused by the next member
+      for (int m = 0; m < G; m++) mask |= act[m] ? 1u << m : 0u;
+      reduce_and_finalize_group<G>(M, mask, L, s0, local_cta, ncta);
     }
   }
 }
@@ -471,18 +472,23 @@ __device__ __forceinline__ void fan_bp_body(const Launch &L) {
       if (threadIdx.x == 0) S.bp_cnt[tile] = 0;
     }
   }
+  double s0[G];
 #pragma unroll
   for (int m = 0; m < G; m++) {
-    if (!act[m]) continue;
-    double s0 = 0.0;
-    if (finish && mine) {
+    s0[m] = 0.0;
+    if (act[m] && finish && mine) {
       const float val = (float)((double)total[m] * ldexp(1.0, -sexp[m]));
-      bp_epilogue(*M[m], L, 0, x, y, val, s0);
+      bp_epilogue(*M[m], L, 0, x, y, val, s0[m]);
     }
-    if (stage_reduces(L.stage)) {
-      double v[1] = {s0};
-      reduce_and_finalize<1>(*M[m], L, v, local_cta, ncta);
-      __syncthreads();  // the shared scratch of the reduction is reused by the next member
+  }
+  if (stage_reduces(L.stage)) {
+    if constexpr (G == 1) {
+      reduce_and_finalize<1>(*M[0], L, s0, local_cta, ncta);
+    } else {
+      unsigned mask = 0;
+#pragma unroll
+      for (int m = 0; m < G; m++) mask |= act[m] ? 1u << m : 0u;
+      reduce_and_finalize_group<G>(M, mask, L, s0, local_cta, ncta);
     }
   }
 }

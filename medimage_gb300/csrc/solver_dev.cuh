@@ -333,6 +333,64 @@ __device__ void reduce_and_finalize(const ScanDev &S, const Launch &L, const dou
   }
 }
 
+// reduce_and_finalize<1> for the members of a projector group at once (member
+// m active when bit m of `act` is set): one barrier pair for all members, the
+// members' partial writes and arrival tickets taken by threads 0..G-1 side by
+// side.  Each member's sum is formed in exactly the order of
+// reduce_and_finalize<1>, so results do not depend on the grouping.
+template <int G>
+__device__ __forceinline__ void reduce_and_finalize_group(const ScanDev *const (&M)[G], unsigned act, const Launch &L,
+                                          const double (&v)[G], int local_cta, int ncta) {
+  __shared__ double red[32][G];
+  __shared__ bool last[G];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int m = 0; m < G; m++) {
+    const double w = warp_sum_d(v[m]);
+    if (lane == 0) red[warp][m] = w;
+  }
+  __syncthreads();
+  // thread m takes member m (static member indices keep M[] in registers)
+#pragma unroll
+  for (int m = 0; m < G; m++) {
+    if (threadIdx.x != m) continue;
+    bool is_last = false;
+    if ((act >> m) & 1u) {
+      double a = 0;
+      for (int w = 0; w < nw; w++) a += red[w][m];
+      const ScanDev &S = *M[m];
+      S.partials[local_cta] = a;
+      __threadfence();
+      const unsigned t = atomicAdd(&S.ctl->arrive, 1u);
+      is_last = (t == (unsigned)ncta - 1);
+    }
+    last[m] = is_last;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int m = 0; m < G; m++) {
+    if (!last[m]) continue;  // the same for every thread of the CTA
+    __threadfence();
+    const ScanDev &S = *M[m];
+    double acc = 0.0;
+    const volatile double *P = S.partials;
+    for (int c = threadIdx.x; c < ncta; c += blockDim.x) acc += P[c];
+    const double w = warp_sum_d(acc);
+    __syncthreads();  // red[][] is free again
+    if (lane == 0) red[warp][0] = w;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double a = 0;
+      for (int ww = 0; ww < nw; ww++) a += red[ww][0];
+      double tot[1] = {a};
+      S.ctl->arrive = 0u;
+      finalize_stage(S, L, tot);
+      __threadfence();
+    }
+    __syncthreads();
+  }
+}
+
 __device__ __forceinline__ void atomic_max_nonneg(unsigned *addr, float x) {
   atomicMax(addr, __float_as_uint(x));
 }

@@ -184,6 +184,26 @@ __device__ __forceinline__ ConeWalk cone_ray(const ScanDev &S, int64_t ray) {
 
 constexpr int kConeThreads = 128;
 
+// Order in which the projectors take rays: bands of kConeBandRows detector
+// rows, every view of a band before the next band, then rows, then columns
+// (a warp's rays are neighbours in a row).  The rays of one band only cross a
+// slab of the volume a few dozen slices thick (the cone angle is small), so
+// the views in flight share that slab in L2 instead of each view sweeping the
+// whole volume through it.  0 = view-major order (bins in sinogram order).
+constexpr int kConeBandRows = 16;
+
+// the sinogram bin ([view][row][col]) of work item i
+__device__ __forceinline__ int64_t cone_bin_of(const ScanDev &S, int64_t i) {
+  if (kConeBandRows == 0) return i;
+  const int64_t full = (int64_t)kConeBandRows * S.ndy * S.nviews;  // items of one full band
+  const int64_t b = i / full, off = i - b * full;
+  const int rows_b = min(kConeBandRows, S.ndx - (int)b * kConeBandRows);
+  const int64_t per_view = (int64_t)rows_b * S.ndy;
+  const int view = (int)(off / per_view), r2 = (int)(off - view * per_view);
+  const int row = (int)b * kConeBandRows + r2 / S.ndy, col = r2 % S.ndy;
+  return ((int64_t)view * S.ndx + row) * S.ndy + col;
+}
+
 // ---------------------------------------------------------------------------
 // forward
 // ---------------------------------------------------------------------------
@@ -194,9 +214,10 @@ __global__ void __launch_bounds__(kConeThreads) cone_fp_kernel(const Launch L) {
   const int cta0 = L.scans ? __ldg(L.prefix + scan) : 0;
   const int ncta = L.scans ? __ldg(L.prefix + scan + 1) - cta0 : gridDim.x;
   const int local_cta = blockIdx.x - cta0;
-  const int64_t ray = (int64_t)local_cta * kConeThreads + threadIdx.x;
+  const int64_t item = (int64_t)local_cta * kConeThreads + threadIdx.x;
   double s0 = 0.0;
-  if (ray < S.nbins) {
+  if (item < S.nbins) {
+    const int64_t ray = cone_bin_of(S, item);
     const float *__restrict__ vol = S.buf[L.in_buf];
     ConeWalk w = cone_ray(S, ray);
     float acc = 0.f, comp = 0.f, part = 0.f;
@@ -250,9 +271,10 @@ __global__ void __launch_bounds__(kConeThreads) cone_bp_kernel(const Launch L) {
   if (!flow_active(S, L.flow)) return;
   const int cta0 = L.scans ? __ldg(L.prefix + scan) : 0;
   const int local_cta = blockIdx.x - cta0;
-  const int64_t ray = (int64_t)local_cta * kConeThreads + threadIdx.x;
+  const int64_t item = (int64_t)local_cta * kConeThreads + threadIdx.x;
   const int sexp = cone_bp_sexp(S);
-  if (ray >= S.nbins) return;
+  if (item >= S.nbins) return;
+  const int64_t ray = cone_bin_of(S, item);
   const float r = S.buf[L.in_buf][ray];
   if (r == 0.f) return;
   const float rs = r * ldexpf(1.f, sexp);

@@ -143,35 +143,52 @@ __device__ __forceinline__ ConeWalk cone_start(int nx, int ny, int nz, float sx,
   return w;
 }
 
-// tracing.cpp:267-306: calls f(on_grid, voxel, weight) per segment.  Each
-// step crosses one plane of the (nx+1) + (ny+1) + (nz+1) inside the clipped
-// segment, so the walk ends within nx + ny + nz + 3 steps; the bound below is
-// only a guard.
-template <typename F>
-__device__ __forceinline__ void cone_walk(ConeWalk &w, int nx, int ny, int nz, F &&f) {
-  const int64_t sxs = (int64_t)w.sx * ny, szs = (int64_t)w.sz * nx * ny;
-  int64_t addr = (int64_t)w.vz * nx * ny + (int64_t)w.vx * ny + w.vy;
-  const int guard = nx + ny + nz + 16;
-  for (int it = 0; w.lam0 < w.stop && it < guard; it++) {
-    const bool on = (unsigned)w.vx < (unsigned)nx && (unsigned)w.vy < (unsigned)ny && (unsigned)w.vz < (unsigned)nz;
-    // the reference's three-way test (x if lx is the smallest or tied, else y
-    // if ly <= lz, else z) as selects: neighbouring rays step differently, so
-    // branches would run every path for the whole warp
-    const bool bx = (w.lx <= w.ly) & (w.lx <= w.lz);
-    const bool by = !bx & (w.ly <= w.lz);
-    const bool bz = !bx & !by;
-    const float cur = bx ? w.lx : (by ? w.ly : w.lz);
-    f(on, addr, __fsub_rn(cur, w.lam0));
-    w.lam0 = cur;
-    const float nlx = __fadd_rn(w.lx, w.len_x), nly = __fadd_rn(w.ly, w.len_y), nlz = __fadd_rn(w.lz, w.len_z);
-    w.lx = bx ? nlx : w.lx;
-    w.ly = by ? nly : w.ly;
-    w.lz = bz ? nlz : w.lz;
-    w.vx += bx ? w.sx : 0;
-    w.vy += by ? w.sy : 0;
-    w.vz += bz ? w.sz : 0;
-    addr += bx ? sxs : (by ? (int64_t)w.sy : szs);
+// tracing.cpp:267-306: calls f(on_grid, voxel, weight) per segment and
+// end_block() after every 32 segments and once after the last (possibly empty)
+// block.  Each step crosses one plane of the (nx+1) + (ny+1) + (nz+1) inside
+// the clipped segment, so the walk ends within nx + ny + nz + 3 steps; the
+// block bound is only a guard.  Idx is the voxel index type: 32-bit when
+// every index the walk can form fits (cone_index32).
+template <typename Idx, typename F, typename B>
+__device__ __forceinline__ void cone_walk(ConeWalk &w, int nx, int ny, int nz, F &&f, B &&end_block) {
+  const Idx nxy = (Idx)nx * ny;
+  const Idx sxs = (Idx)w.sx * ny, sys = (Idx)w.sy, szs = (Idx)w.sz * nxy;
+  Idx addr = (Idx)w.vz * nxy + (Idx)w.vx * ny + (Idx)w.vy;
+  const int guard = (nx + ny + nz + 16) / 32 + 2;
+  for (int blk = 0; blk < guard; blk++) {
+    int j = 0;
+#pragma unroll 4
+    for (; j < 32; j++) {
+      if (!(w.lam0 < w.stop)) break;
+      const bool on =
+          (unsigned)w.vx < (unsigned)nx && (unsigned)w.vy < (unsigned)ny && (unsigned)w.vz < (unsigned)nz;
+      // the reference's three-way test (x if lx is the smallest or tied, else
+      // y if ly <= lz, else z) as selects: neighbouring rays step
+      // differently, so branches would run every path for the whole warp
+      const bool bx = (w.lx <= w.ly) & (w.lx <= w.lz);
+      const bool by = !bx & (w.ly <= w.lz);
+      const bool bz = !bx & !by;
+      const float cur = bx ? w.lx : (by ? w.ly : w.lz);
+      f(on, addr, __fsub_rn(cur, w.lam0));
+      w.lam0 = cur;
+      const float nlx = __fadd_rn(w.lx, w.len_x), nly = __fadd_rn(w.ly, w.len_y), nlz = __fadd_rn(w.lz, w.len_z);
+      w.lx = bx ? nlx : w.lx;
+      w.ly = by ? nly : w.ly;
+      w.lz = bz ? nlz : w.lz;
+      w.vx += bx ? w.sx : 0;
+      w.vy += by ? w.sy : 0;
+      w.vz += bz ? w.sz : 0;
+      addr += bx ? sxs : (by ? sys : szs);
+    }
+    end_block();
+    if (j < 32) break;
   }
+}
+
+// 32-bit voxel indices hold every index a walk can form (each coordinate one
+// step outside the grid at most)
+__host__ __device__ __forceinline__ bool cone_index32(int n, int nz) {
+  return (int64_t)(nz + 2) * n * n < (int64_t)1 << 31;
 }
 
 __device__ __forceinline__ ConeWalk cone_ray(const ScanDev &S, int64_t ray) {
@@ -221,18 +238,22 @@ __global__ void __launch_bounds__(kConeThreads) cone_fp_kernel(const Launch L) {
     const float *__restrict__ vol = S.buf[L.in_buf];
     ConeWalk w = cone_ray(S, ray);
     float acc = 0.f, comp = 0.f, part = 0.f;
-    int k = 0;
-    if (!w.empty)
-      cone_walk(w, S.n, S.n, S.nz, [&](bool on, int64_t addr, float wt) {
-        float val = 0.f;
-        if (on) val = __ldg(vol + addr);  // off-grid voxels are never read
-        part = fmaf(wt, val, part);
-        if ((++k & 31) == 0) {
-          kahan_add(acc, comp, part);
-          part = 0.f;
-        }
-      });
-    kahan_add(acc, comp, part);
+    // FP32 products summed per 32 segments, the partial sums Kahan-folded
+    auto seg = [&](bool on, auto addr, float wt) {
+      float val = 0.f;
+      if (on) val = __ldg(vol + addr);  // off-grid voxels are never read
+      part = fmaf(wt, val, part);
+    };
+    auto fold = [&]() {
+      kahan_add(acc, comp, part);
+      part = 0.f;
+    };
+    if (w.empty)
+      fold();
+    else if (cone_index32(S.n, S.nz))
+      cone_walk<int>(w, S.n, S.n, S.nz, seg, fold);
+    else
+      cone_walk<int64_t>(w, S.n, S.n, S.nz, seg, fold);
     fp_epilogue(S, L, (int)ray, acc - comp, s0);
   }
   if (stage_reduces(L.stage)) {
@@ -283,12 +304,17 @@ __global__ void __launch_bounds__(kConeThreads) cone_bp_kernel(const Launch L) {
   ConeWalk w = cone_ray(S, ray);
   if (w.empty) return;
   unsigned long long *acc = S.bp_acc;
-  cone_walk(w, S.n, S.n, S.nz, [&](bool on, int64_t addr, float wt) {
+  auto seg = [&](bool on, auto addr, float wt) {
     if (on) {
       const long long term = (long long)(__float_as_int(fmaf(wt, rs, kMagic)) - kMagicBits);
       atomicAdd(acc + addr, (unsigned long long)term);
     }
-  });
+  };
+  auto none = [] {};
+  if (cone_index32(S.n, S.nz))
+    cone_walk<int>(w, S.n, S.n, S.nz, seg, none);
+  else
+    cone_walk<int64_t>(w, S.n, S.n, S.nz, seg, none);
 }
 
 // per voxel, over the pixel-pass CTAs (8 x 32 tiles of each slice)
@@ -326,10 +352,13 @@ __global__ void cone_count_kernel(const ScanDev S, unsigned long long *segs, uns
   if (ray < S.nbins) {
     ConeWalk w = cone_ray(S, ray);
     if (!w.empty)
-      cone_walk(w, S.n, S.n, S.nz, [&](bool on, int64_t, float) {
-        cnt++;
-        off += on ? 0 : 1;
-      });
+      cone_walk<int64_t>(
+          w, S.n, S.n, S.nz,
+          [&](bool on, int64_t, float) {
+            cnt++;
+            off += on ? 0 : 1;
+          },
+          [] {});
   }
   const unsigned mine = (unsigned)cnt;
   for (int o = 16; o > 0; o >>= 1) {
@@ -348,13 +377,16 @@ __global__ void cone_trace_one_kernel(const ScanDev S, int64_t ray, int cap, int
   ConeWalk w = cone_ray(S, ray);
   int k = 0;
   if (!w.empty)
-    cone_walk(w, S.n, S.n, S.nz, [&](bool, int64_t addr, float wt) {
-      if (k < cap) {
-        pix[k] = (int)addr;
-        wgt[k] = wt;
-      }
-      k++;
-    });
+    cone_walk<int64_t>(
+        w, S.n, S.n, S.nz,
+        [&](bool, int64_t addr, float wt) {
+          if (k < cap) {
+            pix[k] = (int)addr;
+            wgt[k] = wt;
+          }
+          k++;
+        },
+        [] {});
   *count = k;
 }
 

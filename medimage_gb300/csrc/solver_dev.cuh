@@ -308,10 +308,12 @@ __device__ void reduce_and_finalize(const ScanDev &S, const Launch &L, const dou
 #pragma unroll
   for (int i = 0; i < NS; i++) acc[i] = 0.0;
   if (NS > 0) {
-    const volatile double *P = S.partials;
+    // L2 loads (the partials of other CTAs, published by their fences),
+    // several in flight; the sums keep their order
+#pragma unroll 8
     for (int c = threadIdx.x; c < ncta; c += blockDim.x)
 #pragma unroll
-      for (int i = 0; i < NS; i++) acc[i] += P[(size_t)c * NS + i];
+      for (int i = 0; i < NS; i++) acc[i] += __ldcg(S.partials + (size_t)c * NS + i);
 #pragma unroll
     for (int i = 0; i < NS; i++) {
       const double w = warp_sum_d(acc[i]);
@@ -373,8 +375,8 @@ __device__ __forceinline__ void reduce_and_finalize_group(const ScanDev *const (
     __threadfence();
     const ScanDev &S = *M[m];
     double acc = 0.0;
-    const volatile double *P = S.partials;
-    for (int c = threadIdx.x; c < ncta; c += blockDim.x) acc += P[c];
+#pragma unroll 8
+    for (int c = threadIdx.x; c < ncta; c += blockDim.x) acc += __ldcg(S.partials + c);
     const double w = warp_sum_d(acc);
     __syncthreads();  // red[][] is free again
     if (lane == 0) red[warp][0] = w;

@@ -37,7 +37,9 @@ namespace at {
 // member, so the walk (decision bits, crossing arithmetic) and the gathers are
 // shared.  Each member's sum is formed exactly as it would be alone, so
 // results do not depend on the grouping.
-__global__ void __launch_bounds__(256) fp_pack_kernel(const Launch L) {
+// (bins = 0: images over the pixel-pass CTAs; bins = 1: sinograms over the
+// sinogram-pass CTAs, for the grouped back projector)
+__global__ void __launch_bounds__(256) fp_pack_kernel(const Launch L, int bins) {
   const int scan = find_scan(L.prefix, L.nscans, blockIdx.x);
   const ScanDev &S = L.scans[scan];
   if (S.nmem == 0) return;
@@ -51,8 +53,8 @@ __global__ void __launch_bounds__(256) fp_pack_kernel(const Launch L) {
   }
   if (!any) return;
   const int cta0 = __ldg(L.prefix + scan), ncta = __ldg(L.prefix + scan + 1) - cta0;
-  const int npix = S.n * S.n;
-  for (int p = (blockIdx.x - cta0) * blockDim.x + threadIdx.x; p < npix; p += ncta * blockDim.x) {
+  const int count = bins ? S.nbins : S.n * S.n;
+  for (int p = (blockIdx.x - cta0) * blockDim.x + threadIdx.x; p < count; p += ncta * blockDim.x) {
     float v[kGroupMax];
 #pragma unroll
     for (int m = 0; m < kGroupMax; m++) v[m] = src[m] ? __ldg(src[m] + p) : 0.f;
@@ -324,13 +326,15 @@ __device__ __forceinline__ void fan_bp_body(const Launch &L) {
   __shared__ int last_split;
   for (int i = threadIdx.x; i < G * kMemStride; i += blockDim.x) acc[i] = 0;
   int *const my_acc = acc + (lane % C) * kStride;
-  const float *__restrict__ sino[G];
+  // one scan: its sinogram; a group: the members' sinograms interleaved, one
+  // float4 per bin (the lead's pack buffer)
+  const float *__restrict__ sino = M[0]->buf[L.in_buf];
+  const float4 *__restrict__ spack = S.pack;
   const int32_t *toff = S.tile_off + (size_t)(real ? tile : 0) * S.nvb;
   // fixed-point scale from the largest |r| of each member's sinogram (the same
   // in every split of a tile, so split sums add exactly)
 #pragma unroll
   for (int m = 0; m < G; m++) {
-    sino[m] = M[m]->buf[L.in_buf];
     float mx = (act[m] && threadIdx.x < kBpMaxParts) ? M[m]->bpmax[threadIdx.x] : 0.f;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
@@ -371,19 +375,28 @@ __device__ __forceinline__ void fan_bp_body(const Launch &L) {
       int c = b0 + warp * 32;
       uint4 e = (c + lane < b1) ? __ldg(S.run + c + lane) : kZ;
       uint4 h1 = __ldg(reinterpret_cast<const uint4 *>(S.rays + e.x) + 1);
+      auto load_r = [&](unsigned bin, float(&r)[G]) {
+        if constexpr (G == 1) {
+          r[0] = __ldg(sino + bin);
+        } else {
+          static_assert(G == 4, "members are read as one float4");
+          const float4 v = __ldg(spack + bin);
+          r[0] = v.x;
+          r[1] = v.y;
+          r[2] = v.z;
+          r[3] = v.w;
+        }
+      };
       float r0[G];
-#pragma unroll
-      for (int m = 0; m < G; m++) r0[m] = use[m] ? __ldg(sino[m] + e.x) : 0.f;
+      load_r(e.x, r0);
       for (; c < b1; c += blockDim.x) {
         const int cn = c + blockDim.x;
         const uint4 en = (cn + lane < b1) ? __ldg(S.run + cn + lane) : kZ;
         const uint4 h1n = __ldg(reinterpret_cast<const uint4 *>(S.rays + en.x) + 1);
         float rn[G], rs[G];
+        load_r(en.x, rn);
 #pragma unroll
-        for (int m = 0; m < G; m++) {
-          rn[m] = use[m] ? __ldg(sino[m] + en.x) : 0.f;
-          rs[m] = r0[m] * scale[m];
-        }
+        for (int m = 0; m < G; m++) rs[m] = r0[m] * scale[m];
         const bool valid = c + lane < b1;
         const int k_in = (int)(e.y & 0x3fffu), nk = valid ? (int)((e.y >> 14) & 31u) : 0;
         const int cx_in = (int)(e.y >> 19);
@@ -494,8 +507,8 @@ __device__ __forceinline__ void fan_bp_body(const Launch &L) {
 }
 
 __global__ void __launch_bounds__(256) fan_bp_kernel(const Launch L) { fan_bp_body<1, kBpCopies1>(L); }
-// the member arrays need registers: at most 128 per thread, two CTAs per SM
-__global__ void __launch_bounds__(256, 2) fan_bp_group_kernel(const Launch L) {
+// the member arrays need registers: at most 80 per thread, three CTAs per SM
+__global__ void __launch_bounds__(256, 3) fan_bp_group_kernel(const Launch L) {
   fan_bp_body<kGroupMax, kBpCopiesG>(L);
 }
 
@@ -683,8 +696,18 @@ cudaError_t launch_fp(const Launch &L, int kind, int rpt, int nctas, cudaStream_
 // members' inputs are interleaved (over the pixel-pass CTAs of Lpix), then
 // each group's rays are walked once, one ray per thread.
 cudaError_t launch_fp_group(const Launch &L, const Launch &Lpix, int nctas, int pix_nctas, cudaStream_t st) {
-  fp_pack_kernel<<<pix_nctas, 256, 0, st>>>(Lpix);
+  fp_pack_kernel<<<pix_nctas, 256, 0, st>>>(Lpix, 0);
   fan_fp_kernel<1, kGroupMax><<<nctas, 128, 0, st>>>(L);
+  return cudaGetLastError();
+}
+
+// Back projection of a batch whose scans sharing a plan are grouped: the max
+// |r| pass, the members' sinograms interleaved (over the sinogram-pass CTAs
+// of Lsino), then each group's runs walked once.
+cudaError_t launch_bp_group(const Launch &L, const Launch &Lsino, int nctas, int sino_nctas, cudaStream_t st) {
+  sino_absmax_kernel<<<L.nscans * kBpMaxParts, 256, 0, st>>>(L);
+  fp_pack_kernel<<<sino_nctas, 256, 0, st>>>(Lsino, 1);
+  fan_bp_group_kernel<<<nctas, 256, 0, st>>>(L);
   return cudaGetLastError();
 }
 
@@ -699,10 +722,7 @@ cudaError_t launch_bp(const Launch &L, int kind, int nctas, cudaStream_t st, con
     return launch_cone_bp(L, nctas, *Lpix, pix_nctas, st);
   } else {
     sino_absmax_kernel<<<(L.scans ? L.nscans : 1) * kBpMaxParts, 256, 0, st>>>(L);
-    if (L.group > 1)  // scans sharing a plan walk its runs once
-      fan_bp_group_kernel<<<nctas, 256, 0, st>>>(L);
-    else
-      fan_bp_kernel<<<nctas, 256, 0, st>>>(L);
+    fan_bp_kernel<<<nctas, 256, 0, st>>>(L);
   }
   return cudaGetLastError();
 }

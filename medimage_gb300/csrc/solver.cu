@@ -21,6 +21,7 @@ int bp_ctas(const ScanDev &S);
 int pix_ctas(const ScanDev &S);
 cudaError_t launch_fp(const Launch &L, int kind, int rpt, int nctas, cudaStream_t st);
 cudaError_t launch_fp_group(const Launch &L, const Launch &Lpix, int nctas, int pix_nctas, cudaStream_t st);
+cudaError_t launch_bp_group(const Launch &L, const Launch &Lsino, int nctas, int sino_nctas, cudaStream_t st);
 cudaError_t launch_bp(const Launch &L, int kind, int nctas, cudaStream_t st, const Launch *Lpix, int pix_nctas);
 cudaError_t launch_pixel(int which, const Launch &L, int nctas, cudaStream_t st);
 cudaError_t launch_flags(const ScanDev *scans, int nscans, int mode, cudaStream_t st);
@@ -86,7 +87,7 @@ ScanLayout layout_of(const Plan &p, int rpt) {
   L.bp_bytes = bp_scratch_bytes(p);
   // fan beam and ray tables: a group's forward-projector inputs, interleaved
   const bool packs = p.kind == AT_GEOM_FAN || p.kind == AT_GEOM_RAYS;
-  L.pack_bytes = packs ? align_up(sizeof(float4) * (size_t)p.n * p.n) : 0;
+  L.pack_bytes = packs ? align_up(sizeof(float4) * std::max((size_t)p.n * p.n, nbins)) : 0;
   L.total = L.img_bytes * B_NIMG + L.sino_bytes * (B_NBUF - B_NIMG) + L.partial_bytes + L.trace_bytes +
             L.bp_bytes + L.pack_bytes + align_up(sizeof(Ctl));
   return L;
@@ -240,6 +241,13 @@ int Batch::enqueue_fp(const Launch &L, cudaStream_t st) {
 }
 
 int Batch::enqueue_bp(const Launch &L, cudaStream_t st) {
+  if (group > 1) {  // max |r|, interleave each group's sinograms, then one run walk per group
+    Launch Ls = L;
+    Ls.prefix = prefix_d + FAM_SINO * (nscans + 1);
+    AT_CUDA_TRY(launch_bp_group(L, Ls, bp_total, sino_total, st));
+    launches += 3;
+    return AT_OK;
+  }
   Launch Lp = L;  // the per-pixel finishing pass of the cone-beam back projector
   Lp.prefix = prefix_d + FAM_PIX * (nscans + 1);
   AT_CUDA_TRY(launch_bp(L, kind, bp_total, st, &Lp, pix_total));
@@ -416,7 +424,8 @@ int ProjSet::create(const std::vector<Plan *> &pl) {
   rpt = Solver::choose_rpt(pl);
   const int n = (int)pl.size();
   auto pack_of = [](const Plan &p) {
-    return (p.kind == AT_GEOM_FAN || p.kind == AT_GEOM_RAYS) ? align_up(sizeof(float4) * (size_t)p.n * p.n) : 0;
+    const size_t elems = std::max((size_t)p.n * p.n, (size_t)p.nviews * p.ndets);
+    return (p.kind == AT_GEOM_FAN || p.kind == AT_GEOM_RAYS) ? align_up(sizeof(float4) * elems) : 0;
   };
   size_t total = 256;
   for (auto *p : pl) total += bp_scratch_bytes(*p) + pack_of(*p);

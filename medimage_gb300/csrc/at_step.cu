@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(256) pp_kernel(const Launch L) {
   float *__restrict__ pn = S.buf[L.out_buf];
   const bool first = L.flag != 0;
   const float c2 = first ? 0.f : (float)S.ctl->c2;
-  double sums[2] = {0.0, 0.0};
+  FF sums[2] = {ff_zero(), ff_zero()};
   if (c.inside) {
     auto pnew = [&](int j) -> float { return first ? d[j] : fmaf(c2, po[j], d[j]); };
     const float dc = d[c.i];
@@ -133,17 +133,17 @@ __global__ void __launch_bounds__(256) pp_kernel(const Launch L) {
     pn[c.i] = pc;
     const float pu = c.x > 0 ? pnew(c.i - n) : 0.f;
     const float pl = c.y > 0 ? pnew(c.i - 1) : 0.f;
-    const double vv = (double)v[c.i];
-    const double eps = S.ctl->eps;
-    const double a = (double)pc - pu, b = (double)pc - pl;
+    const float vv = v[c.i];
+    const float eps2 = (float)(0.01 * S.ctl->eps * S.ctl->eps);
+    const float a = pc - pu, b = pc - pl;  // non-negative terms, rounded in FP32
     if (S.nz == 1) {
-      sums[0] = (vv * vv + 0.01 * eps * eps) * (a * a + b * b);
+      sums[0] = ff_of(fmaf(vv, vv, eps2) * fmaf(a, a, b * b));
     } else {
       const float pf = c.z > 0 ? pnew(c.i - n * n) : 0.f;
-      const double cz = (double)pc - pf;
-      sums[0] = (vv * vv + 0.01 * eps * eps) * (a * a + b * b + cz * cz);
+      const float cz = pc - pf;
+      sums[0] = ff_of(fmaf(vv, vv, eps2) * fmaf(a, a, fmaf(b, b, cz * cz)));
     }
-    sums[1] = (double)pc * (double)dc;
+    sums[1] = ff_prod(pc, dc);  // exact
   }
   reduce_and_finalize<2>(S, L, sums, local_cta, ncta);
 }
@@ -186,7 +186,7 @@ __global__ void __launch_bounds__(256) edge_d_kernel(const Launch L) {
   const Ctl *ct = S.ctl;
   const float alpha = (float)ct->alpha, beq = (float)(ct->beta * ct->eps);
   const float b4 = (float)(ct->beta / (4 * ct->eps));
-  double sums[3] = {0.0, 0.0, 0.0};
+  FF sums[3] = {ff_zero(), ff_zero(), ff_zero()};
   if (c.inside && S.nz == 1) {
     auto vat = [&](int xx, int yy) -> float {
       return (xx >= 0 && xx < n && yy >= 0 && yy < n) ? v[xx * n + yy] : 1.f;
@@ -200,12 +200,12 @@ __global__ void __launch_bounds__(256) edge_d_kernel(const Launch L) {
     };
     const float dc = dat(c.x, c.y);
     S.buf[B_D][c.i] = dc;
-    const double dd = (double)dc * dc;
-    sums[0] = dd;
-    sums[1] = (double)nn[c.i] * dd;
-    const double gx = 0.5 * ((double)dat(c.x + 1, c.y) - (double)dat(c.x - 1, c.y));
-    const double gy = 0.5 * ((double)dat(c.x, c.y + 1) - (double)dat(c.x, c.y - 1));
-    sums[2] = gx * gx + gy * gy;
+    // non-negative terms, rounded in FP32 (d^2 exactly)
+    sums[0] = ff_prod(dc, dc);
+    sums[1] = ff_of(nn[c.i] * (dc * dc));
+    const float gx = 0.5f * (dat(c.x + 1, c.y) - dat(c.x - 1, c.y));
+    const float gy = 0.5f * (dat(c.x, c.y + 1) - dat(c.x, c.y - 1));
+    sums[2] = ff_of(fmaf(gx, gx, gy * gy));
   } else if (c.inside) {
     // volumes: six-neighbour Laplacian scaled by 1/6, central differences in z
     const int nz = S.nz;
@@ -223,13 +223,12 @@ __global__ void __launch_bounds__(256) edge_d_kernel(const Launch L) {
     };
     const float dc = dat(c.z, c.x, c.y);
     S.buf[B_D][c.i] = dc;
-    const double dd = (double)dc * dc;
-    sums[0] = dd;
-    sums[1] = (double)nn[c.i] * dd;
-    const double gx = 0.5 * ((double)dat(c.z, c.x + 1, c.y) - (double)dat(c.z, c.x - 1, c.y));
-    const double gy = 0.5 * ((double)dat(c.z, c.x, c.y + 1) - (double)dat(c.z, c.x, c.y - 1));
-    const double gz = 0.5 * ((double)dat(c.z + 1, c.x, c.y) - (double)dat(c.z - 1, c.x, c.y));
-    sums[2] = gx * gx + gy * gy + gz * gz;
+    sums[0] = ff_prod(dc, dc);
+    sums[1] = ff_of(nn[c.i] * (dc * dc));
+    const float gx = 0.5f * (dat(c.z, c.x + 1, c.y) - dat(c.z, c.x - 1, c.y));
+    const float gy = 0.5f * (dat(c.z, c.x, c.y + 1) - dat(c.z, c.x, c.y - 1));
+    const float gz = 0.5f * (dat(c.z + 1, c.x, c.y) - dat(c.z - 1, c.x, c.y));
+    sums[2] = ff_of(fmaf(gx, gx, fmaf(gy, gy, gz * gz)));
   }
   reduce_and_finalize<3>(S, L, sums, local_cta, ncta);
 }
@@ -256,21 +255,21 @@ __global__ void __launch_bounds__(256) edge_upd_kernel(const Launch L) {
 __global__ void __launch_bounds__(256) sino_kernel(const Launch L) {
   AT_SCAN_PROLOGUE
   const int b = local_cta * 256 + threadIdx.x;
-  double s[1] = {0.0};
+  FF s[1] = {ff_zero()};
   if (b < S.nbins) {
     float *q = S.buf[B_Q];
     if (L.stage == ST_SQ) {
       const float qn = fmaf((float)S.ctl->c2, q[b], S.buf[B_AD][b]);
       q[b] = qn;
-      s[0] = (double)qn * qn;
+      s[0] = ff_prod(qn, qn);
     } else {
       const float c1 = (float)S.ctl->c1;
       const float qb = q[b];
       const float af = fmaf(c1, qb, S.buf[B_AF][b]);
       S.buf[B_AF][b] = af;
       S.buf[B_R][b] = S.buf[B_R][b] - c1 * qb;
-      const double dv = (double)af - (double)S.buf[B_G][b];
-      s[0] = dv * dv;
+      const float dv = af - S.buf[B_G][b];
+      s[0] = ff_prod(dv, dv);
     }
   }
   reduce_and_finalize<1>(S, L, s, local_cta, ncta);

@@ -232,7 +232,7 @@ __global__ void __launch_bounds__(kConeThreads) cone_fp_kernel(const Launch L) {
   const int ncta = L.scans ? __ldg(L.prefix + scan + 1) - cta0 : gridDim.x;
   const int local_cta = blockIdx.x - cta0;
   const int64_t item = (int64_t)local_cta * kConeThreads + threadIdx.x;
-  double s0 = 0.0;
+  FF s0 = ff_zero();
   if (item < S.nbins) {
     const int64_t ray = cone_bin_of(S, item);
     const float *__restrict__ vol = S.buf[L.in_buf];
@@ -257,7 +257,7 @@ __global__ void __launch_bounds__(kConeThreads) cone_fp_kernel(const Launch L) {
     fp_epilogue(S, L, (int)ray, acc - comp, s0);
   }
   if (stage_reduces(L.stage)) {
-    double v[1] = {s0};
+    FF v[1] = {s0};
     reduce_and_finalize<1>(S, L, v, local_cta, ncta);
   }
 }
@@ -329,7 +329,7 @@ __global__ void __launch_bounds__(256) cone_bp_finish_kernel(const Launch L) {
   const int z = local_cta / tiles, t = local_cta % tiles;
   const int x = (t / tiles_y) * 8 + (threadIdx.x >> 5), y = (t % tiles_y) * 32 + (threadIdx.x & 31);
   const int sexp = cone_bp_sexp(S);
-  double s0 = 0.0;
+  FF s0 = ff_zero();
   if (x < n && y < n && z < S.nz) {
     const int64_t i = ((int64_t)z * n + x) * n + y;
     const long long total = (long long)atomicExch(S.bp_acc + i, 0ull);
@@ -337,7 +337,7 @@ __global__ void __launch_bounds__(256) cone_bp_finish_kernel(const Launch L) {
     bp_epilogue(S, L, z, x, y, val, s0);
   }
   if (stage_reduces(L.stage)) {
-    double v[1] = {s0};
+    FF v[1] = {s0};
     reduce_and_finalize<1>(S, L, v, local_cta, ncta);
   }
 }

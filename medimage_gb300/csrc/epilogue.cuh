@@ -9,31 +9,33 @@ namespace at {
 // ---------------------------------------------------------------------------
 // epilogues
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void fp_epilogue(const ScanDev &S, const Launch &L, int bin, float val, double &s0) {
+// Sums are float-float (FF): squares and products of floats are exact;
+// val - g is rounded once to FP32 before it is squared.
+__device__ __forceinline__ void fp_epilogue(const ScanDev &S, const Launch &L, int bin, float val, FF &s0) {
   switch (L.stage) {
     case ST_FP0: {  // r = g - Af ; E_data
       const float g = S.buf[B_G][bin];
-      S.buf[B_R][bin] = g - val;
-      const double dv = (double)val - (double)g;
-      s0 += dv * dv;
+      const float rr = g - val;
+      S.buf[B_R][bin] = rr;
+      ff_acc(s0, ff_prod(rr, rr));
       if (L.aux_buf >= 0) S.buf[L.aux_buf][bin] = val;
       break;
     }
     case ST_FPQ:  // q = A p ; |q|^2
       S.buf[B_Q][bin] = val;
-      s0 += (double)val * (double)val;
+      ff_acc(s0, ff_prod(val, val));
       break;
     case ST_FPA: {  // E_data ; r -= c1 q
       const float g = S.buf[B_G][bin];
-      const double dv = (double)val - (double)g;
-      s0 += dv * dv;
+      const float dv = val - g;
+      ff_acc(s0, ff_prod(dv, dv));
       const float c1 = (float)S.ctl->c1;
       S.buf[B_R][bin] = S.buf[B_R][bin] - c1 * S.buf[B_Q][bin];
       if (L.aux_buf >= 0) S.buf[L.aux_buf][bin] = val;
       break;
     }
     case ST_FPD:  // <A d, q>
-      s0 += (double)val * (double)S.buf[B_Q][bin];
+      ff_acc(s0, ff_prod(val, S.buf[B_Q][bin]));
       if (L.aux_buf >= 0) S.buf[L.aux_buf][bin] = val;
       break;
     default:
@@ -51,7 +53,7 @@ __device__ __forceinline__ bool stage_reduces(int stage) {
 // energy over the interior (main.c:135-139, 203-208), for an image (z = 0,
 // nz = 1) or slice z of a volume.
 __device__ __forceinline__ void bp_epilogue(const ScanDev &S, const Launch &L, int z, int x, int y, float val,
-                                            double &s0) {
+                                            FF &s0) {
   const int n = S.n;
   const int i = (z * n + x) * n + y;
   if (L.stage != ST_BP0 && L.stage != ST_BPD) {
@@ -77,8 +79,8 @@ __device__ __forceinline__ void bp_epilogue(const ScanDev &S, const Launch &L, i
                      eps2 * (Td + Tr - 4.f * Tc + Tu + Tl);
     S.buf[B_D][i] = val + alpha * st;
     if (x >= 1 && x <= n - 2 && y >= 1 && y <= n - 2) {
-      const double a = (double)Tc - (double)Tu, b = (double)Tc - (double)Tl;
-      s0 += (double)alpha * ((double)Pc2 + (double)eps2) * (a * a + b * b);
+      const float a = Tc - Tu, b = Tc - Tl;  // a non-negative term, rounded in FP32
+      ff_acc(s0, ff_of(alpha * (Pc2 + eps2) * fmaf(a, a, b * b)));
     }
     return;
   }
@@ -92,8 +94,8 @@ __device__ __forceinline__ void bp_epilogue(const ScanDev &S, const Launch &L, i
                    Pl * Pl * (Tc - Tl) - Pf * Pf * (Tc - Tf) + eps2 * (Td + Tr + Tb - 6.f * Tc + Tu + Tl + Tf);
   S.buf[B_D][i] = val + alpha * st;
   if (x >= 1 && x <= n - 2 && y >= 1 && y <= n - 2 && z >= 1 && z <= S.nz - 2) {
-    const double a = (double)Tc - (double)Tu, b = (double)Tc - (double)Tl, cz = (double)Tc - (double)Tf;
-    s0 += (double)alpha * ((double)Pc2 + (double)eps2) * (a * a + b * b + cz * cz);
+    const float a = Tc - Tu, b = Tc - Tl, cz = Tc - Tf;
+    ff_acc(s0, ff_of(alpha * (Pc2 + eps2) * fmaf(a, a, fmaf(b, b, cz * cz))));
   }
 }
 

@@ -85,9 +85,9 @@ __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
   const int lw = local_cta * 4 + (threadIdx.x >> 5);
   const int blk = lw / kWarpsPerBlock, slice = lw % kWarpsPerBlock;
   const int nblk = S.nviews * S.nbpv;
-  double s0[G];
+  FF s0[G];
 #pragma unroll
-  for (int m = 0; m < G; m++) s0[m] = 0.0;
+  for (int m = 0; m < G; m++) s0[m] = ff_zero();
   if (blk < nblk) {
     const int view = blk / S.nbpv;
     const int in_blk = slice * 32 * RPT + lane * RPT;  // first ray of this thread within the block
@@ -485,10 +485,10 @@ __device__ __forceinline__ void fan_bp_body(const Launch &L) {
       if (threadIdx.x == 0) S.bp_cnt[tile] = 0;
     }
   }
-  double s0[G];
+  FF s0[G];
 #pragma unroll
   for (int m = 0; m < G; m++) {
-    s0[m] = 0.0;
+    s0[m] = ff_zero();
     if (act[m] && finish && mine) {
       const float val = (float)((double)total[m] * ldexp(1.0, -sexp[m]));
       bp_epilogue(*M[m], L, 0, x, y, val, s0[m]);
@@ -553,7 +553,7 @@ __global__ void __launch_bounds__(128) gc_fp_kernel(const Launch L) {
   const int lane = threadIdx.x & 31;
   const int gw = local_cta * 4 + (threadIdx.x >> 5);
   const float *__restrict__ img = S.buf[L.in_buf];
-  double s0 = 0.0;
+  FF s0 = ff_zero();
   if (gw < kGcPairs) {
     const int a = 1 + gw / kGcRays, r = gw % kGcRays;
     float acc[8];
@@ -595,7 +595,7 @@ __global__ void __launch_bounds__(128) gc_fp_kernel(const Launch L) {
     if (lane == 0) fp_epilogue(S, L, view * kGcDets + r, acc, s0);
   }
   if (stage_reduces(L.stage)) {
-    double v[1] = {s0};
+    FF v[1] = {s0};
     reduce_and_finalize<1>(S, L, v, local_cta, ncta);
   }
 }
@@ -638,10 +638,10 @@ __global__ void __launch_bounds__(256) gc_bp_kernel(const Launch L) {
     }
     kahan_add(acc, comp, part);
   }
-  double s0 = 0.0;
+  FF s0 = ff_zero();
   bp_epilogue(S, L, 0, x, y, acc - comp, s0);
   if (stage_reduces(L.stage)) {
-    double v[1] = {s0};
+    FF v[1] = {s0};
     reduce_and_finalize<1>(S, L, v, local_cta, ncta);
   }
 }

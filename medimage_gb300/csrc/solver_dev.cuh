@@ -156,6 +156,49 @@ __device__ __forceinline__ bool flow_active(const ScanDev &S, int flow) {
   return c->edge_active != 0;
 }
 
+// ---- float-float sums ------------------------------------------------------
+// The energy and inner-product reductions are FP64 at the warp level and up,
+// but GB300's FP64 pipe runs at a small fraction of its FP32 rate, and FP64
+// arithmetic per element made the pixel passes FP64-bound.  Per-element terms
+// are therefore formed in FP32 (products of two floats exactly, as hi + lo by
+// one FMA; non-negative terms as one rounded float) and summed across the
+// warp as unevaluated float pairs with error-free additions (Knuth's TwoSum),
+// about 44 bits; the warp total is converted to FP64 once.
+struct FF {
+  float hi, lo;
+};
+__device__ __forceinline__ FF ff_zero() { return FF{0.f, 0.f}; }
+__device__ __forceinline__ FF ff_of(float x) { return FF{x, 0.f}; }
+// a * b exactly
+__device__ __forceinline__ FF ff_prod(float a, float b) {
+  const float p = __fmul_rn(a, b);
+  return FF{p, fmaf(a, b, -p)};
+}
+// s + e == a + b exactly (TwoSum)
+__device__ __forceinline__ FF ff_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return FF{s, e};
+}
+// x + y, renormalised; commutative bit for bit, so a xor butterfly leaves
+// the same total in every lane
+__device__ __forceinline__ FF ff_add(FF x, FF y) {
+  const FF s = ff_two_sum(x.hi, y.hi);
+  const float lo = __fadd_rn(s.lo, __fadd_rn(x.lo, y.lo));
+  const float hi = __fadd_rn(s.hi, lo);
+  return FF{hi, __fsub_rn(lo, __fsub_rn(hi, s.hi))};
+}
+__device__ __forceinline__ void ff_acc(FF &a, FF x) { a = ff_add(a, x); }
+__device__ __forceinline__ double warp_sum_ff(FF v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const FF w{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
+    v = ff_add(v, w);
+  }
+  return (double)v.hi + (double)v.lo;
+}
+
 __device__ __forceinline__ double warp_sum_d(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -271,18 +314,19 @@ __device__ inline void finalize_stage(const ScanDev &S, const Launch &L, const d
   }
 }
 
-// Block-level reduction of NS FP64 values (blockDim.x a multiple of 32, <= 1024),
-// partial write, and the last-CTA finalize.  Must be reached by every thread
-// of the CTA.  `local_cta`/`ncta` index the CTA within its scan.
+// Block-level reduction of NS sums (float-float per thread, FP64 from the warp
+// totals on; blockDim.x a multiple of 32, <= 1024), partial write, and the
+// last-CTA finalize.  Must be reached by every thread of the CTA.
+// `local_cta`/`ncta` index the CTA within its scan.
 template <int NS>
-__device__ void reduce_and_finalize(const ScanDev &S, const Launch &L, const double *v, int local_cta, int ncta) {
+__device__ void reduce_and_finalize(const ScanDev &S, const Launch &L, const FF *v, int local_cta, int ncta) {
   __shared__ double red[32][NS > 0 ? NS : 1];
   __shared__ bool last;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   if (NS > 0) {
 #pragma unroll
     for (int i = 0; i < NS; i++) {
-      const double w = warp_sum_d(v[i]);
+      const double w = warp_sum_ff(v[i]);
       if (lane == 0) red[warp][i] = w;
     }
     __syncthreads();
@@ -342,13 +386,13 @@ __device__ void reduce_and_finalize(const ScanDev &S, const Launch &L, const dou
 // reduce_and_finalize<1>, so results do not depend on the grouping.
 template <int G>
 __device__ __forceinline__ void reduce_and_finalize_group(const ScanDev *const (&M)[G], unsigned act, const Launch &L,
-                                          const double (&v)[G], int local_cta, int ncta) {
+                                          const FF (&v)[G], int local_cta, int ncta) {
   __shared__ double red[32][G];
   __shared__ bool last[G];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
   for (int m = 0; m < G; m++) {
-    const double w = warp_sum_d(v[m]);
+    const double w = warp_sum_ff(v[m]);
     if (lane == 0) red[warp][m] = w;
   }
   __syncthreads();

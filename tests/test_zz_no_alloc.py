@@ -7,8 +7,9 @@ at_forward_residual_noalloc takes its reduction scratch from a fixed array in
 the library.  Here it is called through the C-ABI twice in a row (different
 inputs each time, so the second call starts from the first call's leftovers in
 the shared array) and compared with the existing forward projector, at_forward:
-the residual must match it exactly (same kernel arithmetic), the FP64 energy
-to 1e-12 relative.  This file is collected last on purpose.
+the residual must match it exactly (same kernel arithmetic), and the energy,
+summed from the stored FP32 residual's exact squares, the FP64 sum of those
+squares to 1e-12 relative.  This file is collected last on purpose.
 """
 import ctypes as C
 
@@ -58,7 +59,7 @@ def test_noalloc_forward_residual_matches_forward(engine, kind):
         engine.engine._check("at_forward", L.at_forward(plan.handle, d_img, d_s, None))
         a = _host(L, engine, d_s, (nv, nd), np.float32)
         np.testing.assert_array_equal(r, g - a)
-        ref = float(np.sum((a.astype(np.float64) - g.astype(np.float64)) ** 2))
+        ref = float(np.sum(r.astype(np.float64) ** 2))
         assert abs(energy - ref) <= 1e-12 * ref
     for p in bufs:
         L.at_dev_free(p)

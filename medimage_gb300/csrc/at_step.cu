@@ -48,6 +48,22 @@ __device__ __forceinline__ float warp_max_f(float v) {
   return v;
 }
 
+// max over the CTA into the scan's control block, one atomic per CTA (the
+// scan's CTAs all add to one address).  Thread 0's atomic precedes its fence
+// and arrival ticket in reduce_and_finalize, so the last CTA sees every CTA's
+// maximum.  Must be reached by every thread of the CTA.
+__device__ __forceinline__ void cta_max_to_ctl(const ScanDev &S, float x) {
+  __shared__ float wm[32];
+  x = warp_max_f(x);
+  if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = x;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float m = wm[0];
+    for (int w = 1; w < (int)(blockDim.x >> 5); w++) m = fmaxf(m, wm[w]);
+    if (m > 0.f) atomic_max_nonneg(&S.ctl->maxbits, m);
+  }
+}
+
 __device__ __forceinline__ void sort2(float &a, float &b) {
   const float lo = fminf(a, b), hi = fmaxf(a, b);
   a = lo;
@@ -107,8 +123,7 @@ __global__ void __launch_bounds__(256) upd_kernel(const Launch L) {
       out[c.i] = median9(w[0], w[1], w[2]);
     }
   }
-  cp = warp_max_f(cp);
-  if ((threadIdx.x & 31) == 0 && cp > 0.f) atomic_max_nonneg(&S.ctl->maxbits, cp);
+  cta_max_to_ctl(S, cp);
   reduce_and_finalize<0>(S, L, nullptr, local_cta, ncta);
 }
 
@@ -245,8 +260,7 @@ __global__ void __launch_bounds__(256) edge_upd_kernel(const Launch L) {
     cd = fabsf(step);
     v[c.i] = fminf(fmaxf(v[c.i] + step, 0.f), 1.f);
   }
-  cd = warp_max_f(cd);
-  if ((threadIdx.x & 31) == 0 && cd > 0.f) atomic_max_nonneg(&S.ctl->maxbits, cd);
+  cta_max_to_ctl(S, cd);
   reduce_and_finalize<0>(S, L, nullptr, local_cta, ncta);
 }
 

@@ -64,6 +64,8 @@ __global__ void __launch_bounds__(256) fp_pack_kernel(const Launch L, int bins) 
 
 template <int RPT, int G>
 __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
+  // single scans: 128 threads; groups: kFpGroupThreads (warps of a CTA wait for
+  // its slowest one at the energy reduction)
   const int scan = L.scans ? find_scan(L.prefix, L.nscans, blockIdx.x) : 0;
   const ScanDev &S = scan_of(L, scan);
   const int nm = L.scans ? S.nmem : 1;
@@ -82,7 +84,7 @@ __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
   const int local_cta = blockIdx.x - cta0;
   constexpr int kWarpsPerBlock = 4 / RPT;  // warps per 128-ray bit block
   const int lane = threadIdx.x & 31;
-  const int lw = local_cta * 4 + (threadIdx.x >> 5);
+  const int lw = local_cta * (int)(blockDim.x >> 5) + (threadIdx.x >> 5);
   const int blk = lw / kWarpsPerBlock, slice = lw % kWarpsPerBlock;
   const int nblk = S.nviews * S.nbpv;
   FF s0[G];
@@ -660,6 +662,13 @@ int fp_ctas(const ScanDev &S, int rpt) {
   return (warps + 3) / 4;
 }
 
+// CTAs of a grouped forward projection (one ray per thread)
+int fp_group_ctas(const ScanDev &S) {
+  if (S.kind != AT_GEOM_FAN && S.kind != AT_GEOM_RAYS) return 0;
+  constexpr int w = kFpGroupThreads / 32;
+  return (S.nviews * S.nbpv * 4 + w - 1) / w;
+}
+
 int bp_ctas(const ScanDev &S) {
   if (S.kind == AT_GEOM_GOLDNC) return (kGcN / 8) * (kGcN / 32);
   if (S.kind == AT_GEOM_CONE) return cone_ctas(S);
@@ -697,7 +706,7 @@ cudaError_t launch_fp(const Launch &L, int kind, int rpt, int nctas, cudaStream_
 // each group's rays are walked once, one ray per thread.
 cudaError_t launch_fp_group(const Launch &L, const Launch &Lpix, int nctas, int pix_nctas, cudaStream_t st) {
   fp_pack_kernel<<<pix_nctas, 256, 0, st>>>(Lpix, 0);
-  fan_fp_kernel<1, kGroupMax><<<nctas, 128, 0, st>>>(L);
+  fan_fp_kernel<1, kGroupMax><<<nctas, kFpGroupThreads, 0, st>>>(L);
   return cudaGetLastError();
 }
 

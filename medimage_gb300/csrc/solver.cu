@@ -17,6 +17,7 @@
 namespace at {
 
 int fp_ctas(const ScanDev &S, int rpt);
+int fp_group_ctas(const ScanDev &S);
 int bp_ctas(const ScanDev &S);
 int pix_ctas(const ScanDev &S);
 cudaError_t launch_fp(const Launch &L, int kind, int rpt, int nctas, cudaStream_t st);
@@ -80,7 +81,7 @@ ScanLayout layout_of(const Plan &p, int rpt) {
   fill_scan_plan(tmp, p);
   tmp.bp_split = kBpMaxSplit;  // size the partials for the largest split
   // and for one ray per thread (what grouped forward projections use)
-  const int maxcta = std::max({fp_ctas(tmp, rpt), fp_ctas(tmp, 1), bp_ctas(tmp), pix_ctas(tmp),
+  const int maxcta = std::max({fp_ctas(tmp, rpt), fp_group_ctas(tmp), bp_ctas(tmp), pix_ctas(tmp),
                                (int)((nbins + 255) / 256)});
   L.partial_bytes = align_up((size_t)maxcta * 4 * sizeof(double));
   L.trace_bytes = align_up((size_t)kTraceCap * 10 * sizeof(double));
@@ -197,11 +198,12 @@ int Batch::set(const ScanDev *scans, int n, int kind_, int rpt_, cudaStream_t st
     const int split = bp_split_for(tiles, nvb);
     for (auto &S : sc) S.bp_split = split;
   }
-  const int frpt = group > 1 ? 1 : rpt;  // the grouped forward projector walks one ray per thread
   scans = sc.data();
   std::vector<int> pref(4 * (n + 1), 0);
   for (int s = 0; s < n; s++) {
-    pref[FAM_FP * (n + 1) + s + 1] = pref[FAM_FP * (n + 1) + s] + (scans[s].nmem ? fp_ctas(scans[s], frpt) : 0);
+    // the grouped forward projector walks one ray per thread
+    const int fpc = group > 1 ? fp_group_ctas(scans[s]) : fp_ctas(scans[s], rpt);
+    pref[FAM_FP * (n + 1) + s + 1] = pref[FAM_FP * (n + 1) + s] + (scans[s].nmem ? fpc : 0);
     pref[FAM_PIX * (n + 1) + s + 1] = pref[FAM_PIX * (n + 1) + s] + pix_ctas(scans[s]);
     pref[FAM_SINO * (n + 1) + s + 1] = pref[FAM_SINO * (n + 1) + s] + (scans[s].nbins + 255) / 256;
     pref[FAM_BP * (n + 1) + s + 1] = pref[FAM_BP * (n + 1) + s] + (scans[s].nmem ? bp_ctas(scans[s]) : 0);

@@ -1,7 +1,7 @@
 """GPU parity of the AT solver against the FP64 oracle restatement of
 origin/GoldenC/src/main.c (pinned bit-for-bit to the reference).
 
-Tolerances (stated by the benchmark spec): final f and v rel-L2 <= 1e-4 and PSNR
+Tolerances: final f and v rel-L2 <= 1e-4 and PSNR
 within 0.05 dB after the same iteration count; the branch trace (exit reasons
 per inner loop) must be identical.
 """

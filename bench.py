@@ -342,6 +342,10 @@ def run_ours(args):
     peak, peak_kind = measured_peak_hbm()
     achieved = kern[dom]["bytes"] / (kern[dom]["ms"] / 1e3) / 1e9
     traffic = profile_traffic(dom)
+    if traffic is not None and "group" in dom:
+        # captured on one group of four slices; each group of a launch streams
+        # the plan once, so DRAM traffic scales with the groups in the launch
+        traffic = int(traffic * ((G + 3) // 4))
     gsegs = S_seg * (fp_calls + bp_calls) * slices / (ms / 1e3) / 1e9
     clocks = clk.summary()
 

@@ -245,7 +245,9 @@ int at_rowaction_trace(const at_rowaction *ra, int32_t view, int32_t ray, int32_
                        int32_t *n_out);
 /* msbeam's projection A (proj.c:14-32) on the same traces: d_g = A d_f */
 int at_rowaction_forward(const at_rowaction *ra, int32_t nslices, const float *d_f, float *d_g, void *stream);
-/* f = 0, v = 1, then the sweeps (main.c:364-394); device buffers on `stream` */
+/* f = 0, v = 1, then the sweeps (main.c:364-394); device buffers on `stream`.
+ * The run is captured once as a CUDA graph and replayed while the slice count,
+ * buffers and parameters stay the same; calls on one handle run in order. */
 int at_rowaction_run(const at_rowaction *ra, int32_t nslices, const float *d_g, float *d_f, float *d_v,
                      const at_rowaction_params *prm, void *stream);
 

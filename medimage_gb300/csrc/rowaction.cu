@@ -288,6 +288,23 @@ __global__ void ra_init_kernel(float *f, float *v, size_t n) {
 }  // namespace
 }  // namespace at
 
+// A run is one launch per (sweep, view, phase), a few microseconds of work
+// each, so it is captured as a CUDA graph and replayed; the graph is kept for
+// the next call with the same slice count, buffers and parameters.
+struct RaGraphKey {
+  int nslices = 0;
+  const float *g = nullptr;
+  float *f = nullptr, *v = nullptr;
+  float alpha = 0.f, lambda0 = 0.f, lambda_decay = 0.f;
+  double beta = 0.0, epsilon = 0.0;
+  int sweeps = -1, phases = 0;
+  bool operator==(const RaGraphKey &o) const {
+    return nslices == o.nslices && g == o.g && f == o.f && v == o.v && alpha == o.alpha && lambda0 == o.lambda0 &&
+           lambda_decay == o.lambda_decay && beta == o.beta && epsilon == o.epsilon && sweeps == o.sweeps &&
+           phases == o.phases;
+  }
+};
+
 struct at_rowaction {
   at::RaGeom G{};
   float2 *trig = nullptr;
@@ -295,7 +312,17 @@ struct at_rowaction {
   int *line = nullptr;
   float *weight = nullptr;
   int64_t segments = 0;
+  // the captured run (see RaGraphKey); calls on one handle are serialised by
+  // the graph's launches
+  mutable cudaGraphExec_t exec = nullptr;
+  mutable RaGraphKey key{};
+  mutable cudaStream_t cap = nullptr;
+  mutable cudaEvent_t done = nullptr;  // after the last launch of `exec`
   ~at_rowaction() {
+    if (done) cudaEventSynchronize(done);
+    if (exec) cudaGraphExecDestroy(exec);
+    if (done) cudaEventDestroy(done);
+    if (cap) cudaStreamDestroy(cap);
     cudaFree(trig);
     cudaFree(off);
     cudaFree(line);
@@ -304,6 +331,44 @@ struct at_rowaction {
 };
 
 using namespace at;
+
+namespace {
+// msbeam's run (main.c:365-394): f = 0, v = 1, then `sweeps` sweeps of every
+// view's rays, phase by phase, the step length shrinking after each sweep
+void enqueue_run(const at_rowaction &ra, int nslices, const float *d_g, float *d_f, float *d_v,
+                 const at_rowaction_params &prm, cudaStream_t st) {
+  const size_t npix = (size_t)ra.G.n * ra.G.n * nslices;
+  ra_init_kernel<<<(unsigned)((npix + 255) / 256), 256, 0, st>>>(d_f, d_v, npix);  // main.c:365-369
+  RaArgs A;
+  std::memset(&A, 0, sizeof(A));
+  A.G = ra.G;
+  A.off = ra.off;
+  A.line = ra.line;
+  A.weight = ra.weight;
+  A.g = d_g;
+  A.f = d_f;
+  A.v = d_v;
+  A.phases = prm.phases;
+  A.alpha = prm.alpha;
+  const float epsf = prm.epsilon;
+  A.eps2 = epsf * epsf;
+  A.beta4e = prm.beta / (4 * prm.epsilon);
+  A.betaeps = prm.beta * prm.epsilon;
+  float lambda = prm.lambda0;
+  for (int it = 0; it < prm.sweeps; it++) {
+    A.lambda = lambda;
+    for (int view = 0; view < ra.G.nproj; view++)
+      for (int ph = 0; ph < prm.phases; ph++) {
+        A.view = view;
+        A.phase = ph;
+        A.rays_in_phase = (ra.G.nray - ph + prm.phases - 1) / prm.phases;
+        dim3 grid(A.rays_in_phase, nslices);
+        ra_step_kernel<<<grid, kRaThreads, 0, st>>>(A);
+      }
+    lambda = lambda / (1 + prm.lambda_decay * lambda);  // main.c:391
+  }
+}
+}  // namespace
 
 #define AT_API extern "C" __attribute__((visibility("default")))
 
@@ -386,37 +451,40 @@ AT_API int at_rowaction_run(const at_rowaction *ra, int32_t nslices, const float
   if (prm->sweeps < 0 || prm->phases < 3 || prm->phases > ra->G.nray)
     return set_error(AT_EINVAL, "at_rowaction_run: need sweeps >= 0 and phases >= 3 (rays closer than 3 apart share pixels)");
   cudaStream_t st = (cudaStream_t)stream;
-  const size_t npix = (size_t)ra->G.n * ra->G.n * nslices;
-  ra_init_kernel<<<(unsigned)((npix + 255) / 256), 256, 0, st>>>(d_f, d_v, npix);  // main.c:365-369
-  AT_CUDA_TRY(cudaGetLastError());
-  RaArgs A;
-  std::memset(&A, 0, sizeof(A));
-  A.G = ra->G;
-  A.off = ra->off;
-  A.line = ra->line;
-  A.weight = ra->weight;
-  A.g = d_g;
-  A.f = d_f;
-  A.v = d_v;
-  A.phases = prm->phases;
-  A.alpha = prm->alpha;
-  const float epsf = prm->epsilon;
-  A.eps2 = epsf * epsf;
-  A.beta4e = prm->beta / (4 * prm->epsilon);
-  A.betaeps = prm->beta * prm->epsilon;
-  float lambda = prm->lambda0;
-  for (int it = 0; it < prm->sweeps; it++) {
-    A.lambda = lambda;
-    for (int view = 0; view < ra->G.nproj; view++)
-      for (int ph = 0; ph < prm->phases; ph++) {
-        A.view = view;
-        A.phase = ph;
-        A.rays_in_phase = (ra->G.nray - ph + prm->phases - 1) / prm->phases;
-        dim3 grid(A.rays_in_phase, nslices);
-        ra_step_kernel<<<grid, kRaThreads, 0, st>>>(A);
-      }
-    AT_CUDA_TRY(cudaGetLastError());
-    lambda = lambda / (1 + prm->lambda_decay * lambda);  // main.c:391
+  RaGraphKey key;
+  key.nslices = nslices;
+  key.g = d_g;
+  key.f = d_f;
+  key.v = d_v;
+  key.alpha = prm->alpha;
+  key.lambda0 = prm->lambda0;
+  key.lambda_decay = prm->lambda_decay;
+  key.beta = prm->beta;
+  key.epsilon = prm->epsilon;
+  key.sweeps = prm->sweeps;
+  key.phases = prm->phases;
+  if (!ra->exec || !(ra->key == key)) {
+    if (ra->exec) {
+      AT_CUDA_TRY(cudaEventSynchronize(ra->done));  // its last launch has ended
+      cudaGraphExecDestroy(ra->exec);
+    }
+    ra->exec = nullptr;
+    if (!ra->cap) AT_CUDA_TRY(cudaStreamCreateWithFlags(&ra->cap, cudaStreamNonBlocking));
+    if (!ra->done) AT_CUDA_TRY(cudaEventCreateWithFlags(&ra->done, cudaEventDisableTiming));
+    AT_CUDA_TRY(cudaStreamBeginCapture(ra->cap, cudaStreamCaptureModeThreadLocal));
+    enqueue_run(*ra, nslices, d_g, d_f, d_v, *prm, ra->cap);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(ra->cap, &graph);
+    if (e != cudaSuccess) return cuda_error(e, "at_rowaction_run: capture");
+    const cudaError_t ei = cudaGraphInstantiate(&ra->exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ei != cudaSuccess) {
+      ra->exec = nullptr;
+      return cuda_error(ei, "at_rowaction_run: graph instantiation");
+    }
+    ra->key = key;
   }
+  AT_CUDA_TRY(cudaGraphLaunch(ra->exec, st));
+  AT_CUDA_TRY(cudaEventRecord(ra->done, st));
   return AT_OK;
 }

@@ -76,3 +76,23 @@ def test_batch_slices_equal_alone(engine, ra, oracle):
 def test_rejects_interfering_phases(engine, ra):
     with pytest.raises(engine.AtError):
         ra.run(np.zeros((180, 768), np.float32), engine.RowActionParams(sweeps=1, phases=2))
+
+
+def test_replayed_graph_follows_inputs_and_parameters(engine, ra, oracle):
+    """A run is captured once and replayed while slice count, buffers and
+    parameters stay the same: a replay on new data in the same buffers, and a
+    run with other parameters, must equal fresh host-buffer runs."""
+    torch = pytest.importorskip("torch")
+    ph = oracle.ms_phantom()
+    gs = [oracle.ms_A(ph), oracle.ms_A(np.ascontiguousarray(ph[:, ::-1]))]
+    d_g = torch.empty((180, 768), dtype=torch.float32, device="cuda")
+    d_f = torch.empty((512, 512), dtype=torch.float32, device="cuda")
+    d_v = torch.empty_like(d_f)
+    for prm in (engine.RowActionParams(sweeps=1), engine.RowActionParams(sweeps=2, phases=5)):
+        for g in gs:  # the second pass replays the graph captured for the first
+            d_g.copy_(torch.from_numpy(np.ascontiguousarray(g, np.float32)))
+            ra.run_dev(1, d_g.data_ptr(), d_f.data_ptr(), d_v.data_ptr(), prm)
+            torch.cuda.synchronize()
+            fa, va = ra.run(g, prm)
+            np.testing.assert_array_equal(d_f.cpu().numpy(), fa)
+            np.testing.assert_array_equal(d_v.cpu().numpy(), va)

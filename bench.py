@@ -373,6 +373,10 @@ def run_ours(args):
                          "peak_source": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
                          "traffic": traffic, "algorithmic_bytes_per_launch": kern[dom]["bytes"],
                          "launch_ms": round(kern[dom]["ms"], 5),
+                         "note": (f"{G} projections per launch (groups of 4 slices share one walk of the plan and "
+                                  "one 16-byte gather per segment); algorithmic bytes count 4 S + 4 R per slice, "
+                                  "images stay in L2, so this is an effective rate; the single-slice kernels "
+                                  "below are the HBM-roofline figures") if "group" in dom else None,
                          "kernels": {k: {"launch_ms": round(v["ms"], 5),
                                          "achieved_gbs": round(v["bytes"] / (v["ms"] / 1e3) / 1e9, 1)}
                                      for k, v in kern.items()}},

@@ -37,8 +37,11 @@ namespace at {
 // member, so the walk (decision bits, crossing arithmetic) and the gathers are
 // shared.  Each member's sum is formed exactly as it would be alone, so
 // results do not depend on the grouping.
-// (bins = 0: images over the pixel-pass CTAs; bins = 1: sinograms over the
-// sinogram-pass CTAs, for the grouped back projector)
+
+// Interleaves each group's projector inputs into the lead's pack buffer, one
+// float4 per element, zeros for absent or finished members: images (bins = 0,
+// over the pixel-pass CTAs) before a grouped forward projection, sinograms
+// (bins = 1, over the sinogram-pass CTAs) before a grouped back projection.
 __global__ void __launch_bounds__(256) fp_pack_kernel(const Launch L, int bins) {
   const int scan = find_scan(L.prefix, L.nscans, blockIdx.x);
   const ScanDev &S = L.scans[scan];
@@ -62,10 +65,10 @@ __global__ void __launch_bounds__(256) fp_pack_kernel(const Launch L, int bins) 
   }
 }
 
+// RPT rays per thread, G scans per walk (1, or a group of kGroupMax); CTAs of
+// 128 threads, kFpGroupThreads for groups
 template <int RPT, int G>
 __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
-  // single scans: 128 threads; groups: kFpGroupThreads (warps of a CTA wait for
-  // its slowest one at the energy reduction)
   const int scan = L.scans ? find_scan(L.prefix, L.nscans, blockIdx.x) : 0;
   const ScanDev &S = scan_of(L, scan);
   const int nm = L.scans ? S.nmem : 1;

@@ -39,13 +39,14 @@ namespace at {
 // results do not depend on the grouping.
 
 // Interleaves each group's projector inputs into the lead's pack buffer, one
-// float4 per element, zeros for absent or finished members: images (bins = 0,
+// float2 per element for a pair, one float4 for three or four members, zeros
+// for absent or finished members: images (bins = 0,
 // over the pixel-pass CTAs) before a grouped forward projection, sinograms
 // (bins = 1, over the sinogram-pass CTAs) before a grouped back projection.
 __global__ void __launch_bounds__(256) fp_pack_kernel(const Launch L, int bins) {
   const int scan = find_scan(L.prefix, L.nscans, blockIdx.x);
   const ScanDev &S = L.scans[scan];
-  if (S.nmem == 0) return;
+  if (S.nmem < 2) return;  // a scan alone is read in place
   const float *src[kGroupMax];
   bool any = false;
 #pragma unroll
@@ -61,12 +62,15 @@ __global__ void __launch_bounds__(256) fp_pack_kernel(const Launch L, int bins) 
     float v[kGroupMax];
 #pragma unroll
     for (int m = 0; m < kGroupMax; m++) v[m] = src[m] ? __ldg(src[m] + p) : 0.f;
-    S.pack[p] = make_float4(v[0], v[1], v[2], v[3]);
+    if (S.nmem == 2)
+      reinterpret_cast<float2 *>(S.pack)[p] = make_float2(v[0], v[1]);
+    else
+      S.pack[p] = make_float4(v[0], v[1], v[2], v[3]);
   }
 }
 
-// RPT rays per thread, G scans per walk (1, or a group of kGroupMax); CTAs of
-// 128 threads, kFpGroupThreads for groups
+// RPT rays per thread; G scans per walk: 1, or a group's 2 or 4 members
+// gathered as one float2 / float4 (three members take the float4 form)
 template <int RPT, int G>
 __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
   const int scan = L.scans ? find_scan(L.prefix, L.nscans, blockIdx.x) : 0;
@@ -97,9 +101,10 @@ __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
     const int view = blk / S.nbpv;
     const int in_blk = slice * 32 * RPT + lane * RPT;  // first ray of this thread within the block
     const int det0 = (blk % S.nbpv) * kRayBlock + in_blk;
-    static_assert(G == 1 || G == 4, "members are gathered as one float or one float4");
+    static_assert(G == 1 || G == 2 || G == 4, "members are gathered as one float, float2 or float4");
     const float *__restrict__ img = M[0]->buf[L.in_buf];
     const float4 *__restrict__ pack = S.pack;
+    const float2 *__restrict__ pack2 = reinterpret_cast<const float2 *>(S.pack);
     const unsigned npix = (unsigned)S.npix;
     int idx[RPT], stx[RPT], sty[RPT], nseg[RPT];
     float ax[RPT], ay[RPT], lx[RPT], ly[RPT], cx[RPT], cy[RPT], prev[RPT], acc[RPT][G], comp[RPT][G];
@@ -175,6 +180,10 @@ __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
             prev[r] = cur;
             if constexpr (G == 1) {
               part[r][0] = fmaf(wt, __ldg(img + idx[r]), part[r][0]);
+            } else if constexpr (G == 2) {
+              const float2 v = __ldg(pack2 + idx[r]);
+              part[r][0] = fmaf(wt, v.x, part[r][0]);
+              part[r][1] = fmaf(wt, v.y, part[r][1]);
             } else {
               const float4 v = __ldg(pack + idx[r]);
               part[r][0] = fmaf(wt, v.x, part[r][0]);
@@ -203,6 +212,11 @@ __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
               float val = 0.f;
               if (on) val = __ldg(img + idx[r]);
               part[r][0] = fmaf(wt, val, part[r][0]);
+            } else if constexpr (G == 2) {
+              float2 v = make_float2(0.f, 0.f);
+              if (on) v = __ldg(pack2 + idx[r]);
+              part[r][0] = fmaf(wt, v.x, part[r][0]);
+              part[r][1] = fmaf(wt, v.y, part[r][1]);
             } else {
               float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
               if (on) v = __ldg(pack + idx[r]);
@@ -246,6 +260,7 @@ __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
     }
   }
 }
+
 
 // ---------------------------------------------------------------------------
 // fan-beam back projection (gather over tile runs)
@@ -383,8 +398,12 @@ __device__ __forceinline__ void fan_bp_body(const Launch &L) {
       auto load_r = [&](unsigned bin, float(&r)[G]) {
         if constexpr (G == 1) {
           r[0] = __ldg(sino + bin);
+        } else if constexpr (G == 2) {
+          const float2 v = __ldg(reinterpret_cast<const float2 *>(spack) + bin);
+          r[0] = v.x;
+          r[1] = v.y;
         } else {
-          static_assert(G == 4, "members are read as one float4");
+          static_assert(G == 4, "members are read as one float, float2 or float4");
           const float4 v = __ldg(spack + bin);
           r[0] = v.x;
           r[1] = v.y;
@@ -515,6 +534,14 @@ __global__ void __launch_bounds__(256) fan_bp_kernel(const Launch L) { fan_bp_bo
 // the member arrays need registers: at most 80 per thread, three CTAs per SM
 __global__ void __launch_bounds__(256, 3) fan_bp_group_kernel(const Launch L) {
   fan_bp_body<kGroupMax, kBpCopiesG>(L);
+}
+// in a batch with groups, the scans alone and the pairs
+__global__ void __launch_bounds__(256, 3) fan_bp_small_kernel(const Launch L) {
+  const ScanDev &S = L.scans[find_scan(L.prefix, L.nscans, blockIdx.x)];
+  if (S.nmem <= 1)
+    fan_bp_body<1, kBpCopiesG>(L);
+  else
+    fan_bp_body<2, kBpCopiesG>(L);
 }
 
 // ---------------------------------------------------------------------------
@@ -706,21 +733,47 @@ cudaError_t launch_fp(const Launch &L, int kind, int rpt, int nctas, cudaStream_
 
 // Forward projection of a batch whose scans sharing a plan are grouped: the
 // members' inputs are interleaved (over the pixel-pass CTAs of Lpix), then
-// each group's rays are walked once, one ray per thread.
-cudaError_t launch_fp_group(const Launch &L, const Launch &Lpix, int nctas, int pix_nctas, cudaStream_t st) {
+// each group's rays are walked once, one ray per thread, in one launch per
+// form: groups of three or four over L's CTAs, scans alone over L1's, pairs
+// over L2's.  Returns the number of launches.
+int launch_fp_group(const Launch &L, const Launch &Lpix, const Launch &L1, const Launch &L2, int nctas, int pix_nctas,
+                    int nctas1, int nctas2, cudaStream_t st) {
+  int n = 1;
   fp_pack_kernel<<<pix_nctas, 256, 0, st>>>(Lpix, 0);
-  fan_fp_kernel<1, kGroupMax><<<nctas, kFpGroupThreads, 0, st>>>(L);
-  return cudaGetLastError();
+  if (nctas > 0) {
+    fan_fp_kernel<1, kGroupMax><<<nctas, kFpGroupThreads, 0, st>>>(L);
+    n++;
+  }
+  if (nctas1 > 0) {
+    fan_fp_kernel<1, 1><<<nctas1, kFpGroupThreads, 0, st>>>(L1);
+    n++;
+  }
+  if (nctas2 > 0) {
+    fan_fp_kernel<1, 2><<<nctas2, kFpGroupThreads, 0, st>>>(L2);
+    n++;
+  }
+  return n;
 }
 
 // Back projection of a batch whose scans sharing a plan are grouped: the max
 // |r| pass, the members' sinograms interleaved (over the sinogram-pass CTAs
-// of Lsino), then each group's runs walked once.
-cudaError_t launch_bp_group(const Launch &L, const Launch &Lsino, int nctas, int sino_nctas, cudaStream_t st) {
+// of Lsino), then each group's runs walked once: groups of three or four over
+// L's CTAs, pairs and scans alone over Lsmall's.  Returns the number of
+// launches.
+int launch_bp_group(const Launch &L, const Launch &Lsino, const Launch &Lsmall, int nctas, int sino_nctas,
+                    int small_nctas, cudaStream_t st) {
+  int n = 2;
   sino_absmax_kernel<<<L.nscans * kBpMaxParts, 256, 0, st>>>(L);
   fp_pack_kernel<<<sino_nctas, 256, 0, st>>>(Lsino, 1);
-  fan_bp_group_kernel<<<nctas, 256, 0, st>>>(L);
-  return cudaGetLastError();
+  if (nctas > 0) {
+    fan_bp_group_kernel<<<nctas, 256, 0, st>>>(L);
+    n++;
+  }
+  if (small_nctas > 0) {
+    fan_bp_small_kernel<<<small_nctas, 256, 0, st>>>(Lsmall);
+    n++;
+  }
+  return n;
 }
 
 // Lpix / pix_nctas: the same launch over pixel-pass CTAs, for kernels whose

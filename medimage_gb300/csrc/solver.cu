@@ -21,8 +21,10 @@ int fp_group_ctas(const ScanDev &S);
 int bp_ctas(const ScanDev &S);
 int pix_ctas(const ScanDev &S);
 cudaError_t launch_fp(const Launch &L, int kind, int rpt, int nctas, cudaStream_t st);
-cudaError_t launch_fp_group(const Launch &L, const Launch &Lpix, int nctas, int pix_nctas, cudaStream_t st);
-cudaError_t launch_bp_group(const Launch &L, const Launch &Lsino, int nctas, int sino_nctas, cudaStream_t st);
+int launch_fp_group(const Launch &L, const Launch &Lpix, const Launch &L1, const Launch &L2, int nctas, int pix_nctas,
+                    int nctas1, int nctas2, cudaStream_t st);
+int launch_bp_group(const Launch &L, const Launch &Lsino, const Launch &Lsmall, int nctas, int sino_nctas,
+                    int small_nctas, cudaStream_t st);
 cudaError_t launch_bp(const Launch &L, int kind, int nctas, cudaStream_t st, const Launch *Lpix, int pix_nctas);
 cudaError_t launch_pixel(int which, const Launch &L, int nctas, cudaStream_t st);
 cudaError_t launch_flags(const ScanDev *scans, int nscans, int mode, cudaStream_t st);
@@ -166,7 +168,7 @@ int Batch::set(const ScanDev *scans, int n, int kind_, int rpt_, cudaStream_t st
     prefix_d = nullptr;
     cap = std::max(n, 2 * cap);
     AT_CUDA_TRY(cudaMalloc(&scans_d, sizeof(ScanDev) * cap));
-    AT_CUDA_TRY(cudaMalloc(&prefix_d, sizeof(int) * 4 * (cap + 1)));
+    AT_CUDA_TRY(cudaMalloc(&prefix_d, sizeof(int) * kFamilies * (cap + 1)));
   }
   nscans = n;
   std::vector<ScanDev> sc(scans, scans + n);
@@ -199,19 +201,36 @@ int Batch::set(const ScanDev *scans, int n, int kind_, int rpt_, cudaStream_t st
     for (auto &S : sc) S.bp_split = split;
   }
   scans = sc.data();
-  std::vector<int> pref(4 * (n + 1), 0);
+  std::vector<int> pref(kFamilies * (n + 1), 0);
+  auto add = [&](int fam, int s, int ctas) { pref[fam * (n + 1) + s + 1] = pref[fam * (n + 1) + s] + ctas; };
   for (int s = 0; s < n; s++) {
-    // the grouped forward projector walks one ray per thread
-    const int fpc = group > 1 ? fp_group_ctas(scans[s]) : fp_ctas(scans[s], rpt);
-    pref[FAM_FP * (n + 1) + s + 1] = pref[FAM_FP * (n + 1) + s] + (scans[s].nmem ? fpc : 0);
-    pref[FAM_PIX * (n + 1) + s + 1] = pref[FAM_PIX * (n + 1) + s] + pix_ctas(scans[s]);
-    pref[FAM_SINO * (n + 1) + s + 1] = pref[FAM_SINO * (n + 1) + s] + (scans[s].nbins + 255) / 256;
-    pref[FAM_BP * (n + 1) + s + 1] = pref[FAM_BP * (n + 1) + s] + (scans[s].nmem ? bp_ctas(scans[s]) : 0);
+    const int nm = scans[s].nmem;
+    if (group > 1) {
+      // grouped projectors walk one ray per thread; groups of three or four
+      // and the rest (pairs, scans alone) in launches of their own
+      const bool big = nm >= 3, small = nm == 1 || nm == 2;
+      add(FAM_FP, s, big ? fp_group_ctas(scans[s]) : 0);
+      add(FAM_FP1, s, nm == 1 ? fp_group_ctas(scans[s]) : 0);
+      add(FAM_FP2, s, nm == 2 ? fp_group_ctas(scans[s]) : 0);
+      add(FAM_BP, s, big ? bp_ctas(scans[s]) : 0);
+      add(FAM_BPS, s, small ? bp_ctas(scans[s]) : 0);
+    } else {
+      add(FAM_FP, s, fp_ctas(scans[s], rpt));
+      add(FAM_FP1, s, 0);
+      add(FAM_FP2, s, 0);
+      add(FAM_BP, s, bp_ctas(scans[s]));
+      add(FAM_BPS, s, 0);
+    }
+    add(FAM_PIX, s, pix_ctas(scans[s]));
+    add(FAM_SINO, s, (scans[s].nbins + 255) / 256);
   }
   fp_total = pref[FAM_FP * (n + 1) + n];
   pix_total = pref[FAM_PIX * (n + 1) + n];
   sino_total = pref[FAM_SINO * (n + 1) + n];
   bp_total = pref[FAM_BP * (n + 1) + n];
+  fp1_total = pref[FAM_FP1 * (n + 1) + n];
+  fp2_total = pref[FAM_FP2 * (n + 1) + n];
+  bps_total = pref[FAM_BPS * (n + 1) + n];
   // pageable sources: the copies are staged before cudaMemcpyAsync returns
   AT_CUDA_TRY(cudaMemcpyAsync(scans_d, scans, sizeof(ScanDev) * n, cudaMemcpyHostToDevice, st));
   AT_CUDA_TRY(cudaMemcpyAsync(prefix_d, pref.data(), sizeof(int) * pref.size(), cudaMemcpyHostToDevice, st));
@@ -225,16 +244,18 @@ Launch Batch::base_launch(int family) const {
   L.nscans = nscans;
   L.prefix = prefix_d + family * (nscans + 1);
   L.aux_buf = -1;
-  L.group = (family == FAM_FP || family == FAM_BP) ? group : 1;
+  L.group = (family == FAM_PIX || family == FAM_SINO) ? 1 : group;
   return L;
 }
 
 int Batch::enqueue_fp(const Launch &L, cudaStream_t st) {
   if (group > 1) {  // interleave each group's inputs, then one walk per group
-    Launch Lp = L;
+    Launch Lp = L, L1 = L, L2 = L;
     Lp.prefix = prefix_d + FAM_PIX * (nscans + 1);
-    AT_CUDA_TRY(launch_fp_group(L, Lp, fp_total, pix_total, st));
-    launches += 2;
+    L1.prefix = prefix_d + FAM_FP1 * (nscans + 1);
+    L2.prefix = prefix_d + FAM_FP2 * (nscans + 1);
+    launches += launch_fp_group(L, Lp, L1, L2, fp_total, pix_total, fp1_total, fp2_total, st);
+    AT_CUDA_TRY(cudaGetLastError());
   } else {
     AT_CUDA_TRY(launch_fp(L, kind, rpt, fp_total, st));
     launches++;
@@ -244,10 +265,11 @@ int Batch::enqueue_fp(const Launch &L, cudaStream_t st) {
 
 int Batch::enqueue_bp(const Launch &L, cudaStream_t st) {
   if (group > 1) {  // max |r|, interleave each group's sinograms, then one run walk per group
-    Launch Ls = L;
+    Launch Ls = L, Lsm = L;
     Ls.prefix = prefix_d + FAM_SINO * (nscans + 1);
-    AT_CUDA_TRY(launch_bp_group(L, Ls, bp_total, sino_total, st));
-    launches += 3;
+    Lsm.prefix = prefix_d + FAM_BPS * (nscans + 1);
+    launches += launch_bp_group(L, Ls, Lsm, bp_total, sino_total, bps_total, st);
+    AT_CUDA_TRY(cudaGetLastError());
     return AT_OK;
   }
   Launch Lp = L;  // the per-pixel finishing pass of the cone-beam back projector

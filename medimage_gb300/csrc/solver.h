@@ -23,7 +23,10 @@ void carve_bp_scratch(ScanDev &S, const Plan &p, char *mem);
 int bp_split_for(int tiles, int nvb);
 
 // CTA-range families of a batch's launches (rows of Batch::prefix_d)
-enum Family { FAM_FP = 0, FAM_PIX = 1, FAM_SINO = 2, FAM_BP = 3 };
+// (in a batch with groups, the projections of the scans alone and of the
+// pairs are launched apart from the groups of three or four: forward
+// FAM_FP1 / FAM_FP2, back FAM_BPS)
+enum Family { FAM_FP = 0, FAM_PIX = 1, FAM_SINO = 2, FAM_BP = 3, FAM_FP1 = 4, FAM_FP2 = 5, FAM_BPS = 6, kFamilies = 7 };
 
 // The launch sequence of the AT iteration over a set of scans: one launch per
 // kernel for the whole set, per-scan CTA ranges from prefix tables.
@@ -31,8 +34,8 @@ struct Batch {
   at_params params{};
   int kind = AT_GEOM_FAN, rpt = 1, nscans = 0, cap = 0;
   ScanDev *scans_d = nullptr;
-  int *prefix_d = nullptr;  // [4][cap+1]: forward-projector, pixel-pass, sinogram-pass, back-projector CTAs
-  int fp_total = 0, pix_total = 0, sino_total = 0, bp_total = 0;
+  int *prefix_d = nullptr;  // [kFamilies][cap+1]: CTAs per scan of each family
+  int fp_total = 0, pix_total = 0, sino_total = 0, bp_total = 0, fp1_total = 0, fp2_total = 0, bps_total = 0;
   int group = 1;            // largest group of scans sharing a plan (projected together)
   int launches = 0;         // kernel launches of the last enqueue_outer
   Batch() = default;

@@ -1,9 +1,11 @@
 // at_step.cu -- pixel and sinogram passes of the AT iteration
 // (origin/GoldenC/src/main.c:81-390) for a batch of scans.
 //
-// Pixel passes use 8 x 32 tiles (x rows, y columns; 256 threads), the same
-// CTA numbering as the back projector, so one prefix table serves both; a
-// volume (nz > 1 slices, the cone beam) has the tiles of each slice in turn.
+// Pixel passes use tiles of kPixRows x 32 pixels (x rows, y columns; 256
+// threads, each taking kPixRows / 8 rows of the tile, 8 apart), so a CTA's
+// fixed costs (control-block reads, its reduction, fence and arrival ticket)
+// are spread over several pixels per thread; a volume (nz > 1 slices, the
+// cone beam) has the tiles of each slice in turn.
 // On volumes the stencils gain the z neighbours (gradients, Laplacian,
 // smoothness energy); the median stays GoldenC's 3x3 within each slice.  Each
 // pass fuses the elementwise update with the reductions the next scalar step
@@ -20,17 +22,25 @@ struct PixCoord {
   bool inside;
 };
 
-__device__ __forceinline__ PixCoord pix_of(int n, int local_cta) {
-  const int tiles_y = (n + 31) >> 5, tiles = ((n + 7) >> 3) * tiles_y;
+// this thread's pixel in row group j (0 <= j < kPixRows / 8) of the CTA's tile
+__device__ __forceinline__ PixCoord pix_of(int n, int local_cta, int j) {
+  const int tiles_y = (n + 31) >> 5, tiles = ((n + kPixRows - 1) / kPixRows) * tiles_y;
   PixCoord c;
   c.z = local_cta / tiles;
   const int t = local_cta % tiles;
-  c.x = (t / tiles_y) * 8 + (threadIdx.x >> 5);
+  c.x = (t / tiles_y) * kPixRows + j * 8 + (threadIdx.x >> 5);
   c.y = (t % tiles_y) * 32 + (threadIdx.x & 31);
   c.inside = c.x < n && c.y < n;
   c.base = c.z * n * n;
   c.i = c.base + c.x * n + c.y;
   return c;
+}
+
+// f(c) for each of this thread's pixels
+template <typename F>
+__device__ __forceinline__ void for_my_pixels(int n, int local_cta, F &&f) {
+#pragma unroll
+  for (int j = 0; j < kPixRows / 8; j++) f(pix_of(n, local_cta, j));
 }
 
 #define AT_SCAN_PROLOGUE                                                              \
@@ -95,15 +105,15 @@ __device__ __forceinline__ float median9(float r0[3], float r1[3], float r2[3]) 
 __global__ void __launch_bounds__(256) upd_kernel(const Launch L) {
   AT_SCAN_PROLOGUE
   const int n = S.n;
-  const PixCoord c = pix_of(n, local_cta);
   const float *__restrict__ u = S.buf[L.aux_buf];
   const float *__restrict__ p = S.buf[L.in_buf];
   float *__restrict__ out = S.buf[L.out_buf];
   const float c1 = (float)S.ctl->c1;
   float cp = 0.f;
-  if (c.inside) {
+  for_my_pixels(n, local_cta, [&](const PixCoord &c) {
+    if (!c.inside) return;
     const float pc = p[c.i];
-    cp = fabsf(c1 * pc);
+    cp = fmaxf(cp, fabsf(c1 * pc));
     if (!L.flag) {
       out[c.i] = fmaf(c1, pc, u[c.i]);
     } else {
@@ -122,7 +132,7 @@ __global__ void __launch_bounds__(256) upd_kernel(const Launch L) {
         }
       out[c.i] = median9(w[0], w[1], w[2]);
     }
-  }
+  });
   cta_max_to_ctl(S, cp);
   reduce_and_finalize<0>(S, L, nullptr, local_cta, ncta);
 }
@@ -133,15 +143,16 @@ __global__ void __launch_bounds__(256) upd_kernel(const Launch L) {
 __global__ void __launch_bounds__(256) pp_kernel(const Launch L) {
   AT_SCAN_PROLOGUE
   const int n = S.n;
-  const PixCoord c = pix_of(n, local_cta);
   const float *__restrict__ d = S.buf[B_D];
   const float *__restrict__ po = S.buf[L.in_buf];
   const float *__restrict__ v = S.buf[B_V];
   float *__restrict__ pn = S.buf[L.out_buf];
   const bool first = L.flag != 0;
   const float c2 = first ? 0.f : (float)S.ctl->c2;
+  const float eps2 = (float)(0.01 * S.ctl->eps * S.ctl->eps);
   FF sums[2] = {ff_zero(), ff_zero()};
-  if (c.inside) {
+  for_my_pixels(n, local_cta, [&](const PixCoord &c) {
+    if (!c.inside) return;
     auto pnew = [&](int j) -> float { return first ? d[j] : fmaf(c2, po[j], d[j]); };
     const float dc = d[c.i];
     const float pc = pnew(c.i);
@@ -149,34 +160,35 @@ __global__ void __launch_bounds__(256) pp_kernel(const Launch L) {
     const float pu = c.x > 0 ? pnew(c.i - n) : 0.f;
     const float pl = c.y > 0 ? pnew(c.i - 1) : 0.f;
     const float vv = v[c.i];
-    const float eps2 = (float)(0.01 * S.ctl->eps * S.ctl->eps);
     const float a = pc - pu, b = pc - pl;  // non-negative terms, rounded in FP32
     if (S.nz == 1) {
-      sums[0] = ff_of(fmaf(vv, vv, eps2) * fmaf(a, a, b * b));
+      ff_acc(sums[0], ff_of(fmaf(vv, vv, eps2) * fmaf(a, a, b * b)));
     } else {
       const float pf = c.z > 0 ? pnew(c.i - n * n) : 0.f;
       const float cz = pc - pf;
-      sums[0] = ff_of(fmaf(vv, vv, eps2) * fmaf(a, a, fmaf(b, b, cz * cz)));
+      ff_acc(sums[0], ff_of(fmaf(vv, vv, eps2) * fmaf(a, a, fmaf(b, b, cz * cz))));
     }
-    sums[1] = ff_prod(pc, dc);  // exact
-  }
+    ff_acc(sums[1], ff_prod(pc, dc));  // exact
+  });
   reduce_and_finalize<2>(S, L, sums, local_cta, ncta);
 }
 
 // F = U1 when the image step ended in update buffer 1.
 __global__ void __launch_bounds__(256) commit_kernel(const Launch L) {
   AT_SCAN_PROLOGUE
-  const PixCoord c = pix_of(S.n, local_cta);
-  if (c.inside && S.ctl->final_u == 1) S.buf[B_F][c.i] = S.buf[B_U1][c.i];
+  if (S.ctl->final_u != 1) return;
+  for_my_pixels(S.n, local_cta, [&](const PixCoord &c) {
+    if (c.inside) S.buf[B_F][c.i] = S.buf[B_U1][c.i];
+  });
 }
 
 // |grad f|^2 with central differences, f zero-padded (main.c:296-298).
 __global__ void __launch_bounds__(256) edge_init_kernel(const Launch L) {
   AT_SCAN_PROLOGUE
   const int n = S.n;
-  const PixCoord c = pix_of(n, local_cta);
-  if (!c.inside) return;
   const float *__restrict__ f = S.buf[B_F];
+  for_my_pixels(n, local_cta, [&](const PixCoord &c) {
+  if (!c.inside) return;
   const float fd = c.x + 1 < n ? f[c.i + n] : 0.f, fu = c.x > 0 ? f[c.i - n] : 0.f;
   const float fr = c.y + 1 < n ? f[c.i + 1] : 0.f, fl = c.y > 0 ? f[c.i - 1] : 0.f;
   const float gx = 0.5f * (fd - fu), gy = 0.5f * (fr - fl);
@@ -188,6 +200,7 @@ __global__ void __launch_bounds__(256) edge_init_kernel(const Launch L) {
     const float gz = 0.5f * (fb - ff);
     S.buf[B_NN][c.i] = gx * gx + gy * gy + gz * gz;
   }
+  });
 }
 
 // d = -(alpha v n - beta eps lap/4 v + beta (v-1)/(4 eps)), v one-padded
@@ -195,13 +208,13 @@ __global__ void __launch_bounds__(256) edge_init_kernel(const Launch L) {
 __global__ void __launch_bounds__(256) edge_d_kernel(const Launch L) {
   AT_SCAN_PROLOGUE
   const int n = S.n;
-  const PixCoord c = pix_of(n, local_cta);
   const float *__restrict__ v = S.buf[B_V];
   const float *__restrict__ nn = S.buf[B_NN];
   const Ctl *ct = S.ctl;
   const float alpha = (float)ct->alpha, beq = (float)(ct->beta * ct->eps);
   const float b4 = (float)(ct->beta / (4 * ct->eps));
   FF sums[3] = {ff_zero(), ff_zero(), ff_zero()};
+  for_my_pixels(n, local_cta, [&](const PixCoord &c) {
   if (c.inside && S.nz == 1) {
     auto vat = [&](int xx, int yy) -> float {
       return (xx >= 0 && xx < n && yy >= 0 && yy < n) ? v[xx * n + yy] : 1.f;
@@ -216,11 +229,11 @@ __global__ void __launch_bounds__(256) edge_d_kernel(const Launch L) {
     const float dc = dat(c.x, c.y);
     S.buf[B_D][c.i] = dc;
     // non-negative terms, rounded in FP32 (d^2 exactly)
-    sums[0] = ff_prod(dc, dc);
-    sums[1] = ff_of(nn[c.i] * (dc * dc));
+    ff_acc(sums[0], ff_prod(dc, dc));
+    ff_acc(sums[1], ff_of(nn[c.i] * (dc * dc)));
     const float gx = 0.5f * (dat(c.x + 1, c.y) - dat(c.x - 1, c.y));
     const float gy = 0.5f * (dat(c.x, c.y + 1) - dat(c.x, c.y - 1));
-    sums[2] = ff_of(fmaf(gx, gx, gy * gy));
+    ff_acc(sums[2], ff_of(fmaf(gx, gx, gy * gy)));
   } else if (c.inside) {
     // volumes: six-neighbour Laplacian scaled by 1/6, central differences in z
     const int nz = S.nz;
@@ -238,28 +251,30 @@ __global__ void __launch_bounds__(256) edge_d_kernel(const Launch L) {
     };
     const float dc = dat(c.z, c.x, c.y);
     S.buf[B_D][c.i] = dc;
-    sums[0] = ff_prod(dc, dc);
-    sums[1] = ff_of(nn[c.i] * (dc * dc));
+    ff_acc(sums[0], ff_prod(dc, dc));
+    ff_acc(sums[1], ff_of(nn[c.i] * (dc * dc)));
     const float gx = 0.5f * (dat(c.z, c.x + 1, c.y) - dat(c.z, c.x - 1, c.y));
     const float gy = 0.5f * (dat(c.z, c.x, c.y + 1) - dat(c.z, c.x, c.y - 1));
     const float gz = 0.5f * (dat(c.z + 1, c.x, c.y) - dat(c.z - 1, c.x, c.y));
-    sums[2] = ff_of(fmaf(gx, gx, fmaf(gy, gy, gz * gz)));
+    ff_acc(sums[2], ff_of(fmaf(gx, gx, fmaf(gy, gy, gz * gz))));
   }
+  });
   reduce_and_finalize<3>(S, L, sums, local_cta, ncta);
 }
 
 // v = clamp(v + c d, 0, 1); maxCD = max |c d| (main.c:332-344).
 __global__ void __launch_bounds__(256) edge_upd_kernel(const Launch L) {
   AT_SCAN_PROLOGUE
-  const PixCoord c = pix_of(S.n, local_cta);
   const float cc = (float)S.ctl->c;
   float cd = 0.f;
-  if (c.inside) {
-    float *v = S.buf[B_V];
-    const float step = cc * S.buf[B_D][c.i];
-    cd = fabsf(step);
+  float *v = S.buf[B_V];
+  const float *dd = S.buf[B_D];
+  for_my_pixels(S.n, local_cta, [&](const PixCoord &c) {
+    if (!c.inside) return;
+    const float step = cc * dd[c.i];
+    cd = fmaxf(cd, fabsf(step));
     v[c.i] = fminf(fmaxf(v[c.i] + step, 0.f), 1.f);
-  }
+  });
   cta_max_to_ctl(S, cd);
   reduce_and_finalize<0>(S, L, nullptr, local_cta, ncta);
 }
@@ -292,10 +307,11 @@ __global__ void __launch_bounds__(256) sino_kernel(const Launch L) {
 // f = 0, v = 1 (main.c:36-40).
 __global__ void __launch_bounds__(256) init_state_kernel(const Launch L) {
   AT_SCAN_PROLOGUE
-  const PixCoord c = pix_of(S.n, local_cta);
-  if (!c.inside) return;
-  S.buf[B_F][c.i] = 0.f;
-  S.buf[B_V][c.i] = 1.f;
+  for_my_pixels(S.n, local_cta, [&](const PixCoord &c) {
+    if (!c.inside) return;
+    S.buf[B_F][c.i] = 0.f;
+    S.buf[B_V][c.i] = 1.f;
+  });
 }
 
 // step boundaries: flag 0 = begin image step, 1 = begin edge step.

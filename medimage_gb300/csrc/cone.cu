@@ -317,7 +317,8 @@ __global__ void __launch_bounds__(kConeThreads) cone_bp_kernel(const Launch L) {
     cone_walk<int64_t>(w, S.n, S.n, S.nz, seg, none);
 }
 
-// per voxel, over the pixel-pass CTAs (8 x 32 tiles of each slice)
+// per voxel, over the pixel-pass CTAs (kPixRows x 32 tiles of each slice,
+// each thread kPixRows / 8 rows 8 apart)
 __global__ void __launch_bounds__(256) cone_bp_finish_kernel(const Launch L) {
   const int scan = L.scans ? find_scan(L.prefix, L.nscans, blockIdx.x) : 0;
   const ScanDev &S = scan_of(L, scan);
@@ -325,16 +326,20 @@ __global__ void __launch_bounds__(256) cone_bp_finish_kernel(const Launch L) {
   const int cta0 = L.scans ? __ldg(L.prefix + scan) : 0;
   const int ncta = L.scans ? __ldg(L.prefix + scan + 1) - cta0 : gridDim.x;
   const int local_cta = blockIdx.x - cta0;
-  const int n = S.n, tiles_y = (n + 31) >> 5, tiles = ((n + 7) >> 3) * tiles_y;
+  const int n = S.n, tiles_y = (n + 31) >> 5, tiles = ((n + kPixRows - 1) / kPixRows) * tiles_y;
   const int z = local_cta / tiles, t = local_cta % tiles;
-  const int x = (t / tiles_y) * 8 + (threadIdx.x >> 5), y = (t % tiles_y) * 32 + (threadIdx.x & 31);
+  const int y = (t % tiles_y) * 32 + (threadIdx.x & 31);
   const int sexp = cone_bp_sexp(S);
   FF s0 = ff_zero();
-  if (x < n && y < n && z < S.nz) {
-    const int64_t i = ((int64_t)z * n + x) * n + y;
-    const long long total = (long long)atomicExch(S.bp_acc + i, 0ull);
-    const float val = (float)((double)total * ldexp(1.0, -sexp));
-    bp_epilogue(S, L, z, x, y, val, s0);
+#pragma unroll
+  for (int j = 0; j < kPixRows / 8; j++) {
+    const int x = (t / tiles_y) * kPixRows + j * 8 + (threadIdx.x >> 5);
+    if (x < n && y < n && z < S.nz) {
+      const int64_t i = ((int64_t)z * n + x) * n + y;
+      const long long total = (long long)atomicExch(S.bp_acc + i, 0ull);
+      const float val = (float)((double)total * ldexp(1.0, -sexp));
+      bp_epilogue(S, L, z, x, y, val, s0);
+    }
   }
   if (stage_reduces(L.stage)) {
     FF v[1] = {s0};

@@ -714,7 +714,7 @@ int bp_split_for(int tiles, int nvb) {
   return std::max(1, std::min({s, nvb, kBpMaxSplit}));
 }
 
-int pix_ctas(const ScanDev &S) { return ((S.n + 7) / 8) * ((S.n + 31) / 32) * S.nz; }
+int pix_ctas(const ScanDev &S) { return ((S.n + kPixRows - 1) / kPixRows) * ((S.n + 31) / 32) * S.nz; }
 
 cudaError_t launch_fp(const Launch &L, int kind, int rpt, int nctas, cudaStream_t st) {
   if (kind == AT_GEOM_GOLDNC) {

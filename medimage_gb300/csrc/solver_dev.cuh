@@ -76,6 +76,7 @@ constexpr int kTraceCap = 4096;  // records per scan (10 doubles each)
 constexpr int kBpMaxParts = 64;  // CTAs of the max |r| pass per scan
 constexpr int kBpMaxSplit = 8;   // most CTAs one back-projection tile is split over
 constexpr int kGroupMax = 4;     // most scans of one plan whose projections share a walk
+constexpr int kPixRows = 32;     // rows of a pixel-pass CTA's tile (32 columns; a multiple of 8)
 constexpr int kFpGroupThreads = 128;  // CTA size of the grouped forward projector (<= 128)
 
 struct ScanDev {

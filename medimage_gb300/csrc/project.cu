@@ -40,7 +40,9 @@ namespace at {
 
 // Interleaves each group's projector inputs into the lead's pack buffer, one
 // float2 per element for a pair, one float4 for three or four members, zeros
-// for absent or finished members: images (bins = 0,
+// for absent or finished members; images twice, row-major and transposed
+// (the forward projector reads whichever puts a warp's neighbouring rays in
+// fewer sectors): images (bins = 0,
 // over the pixel-pass CTAs) before a grouped forward projection, sinograms
 // (bins = 1, over the sinogram-pass CTAs) before a grouped back projection.
 __global__ void __launch_bounds__(256) fp_pack_kernel(const Launch L, int bins) {
@@ -57,15 +59,22 @@ __global__ void __launch_bounds__(256) fp_pack_kernel(const Launch L, int bins) 
   }
   if (!any) return;
   const int cta0 = __ldg(L.prefix + scan), ncta = __ldg(L.prefix + scan + 1) - cta0;
-  const int count = bins ? S.nbins : S.n * S.n;
+  const int n = S.n, npix = n * n;
+  const int count = bins ? S.nbins : npix;
   for (int p = (blockIdx.x - cta0) * blockDim.x + threadIdx.x; p < count; p += ncta * blockDim.x) {
     float v[kGroupMax];
 #pragma unroll
     for (int m = 0; m < kGroupMax; m++) v[m] = src[m] ? __ldg(src[m] + p) : 0.f;
-    if (S.nmem == 2)
-      reinterpret_cast<float2 *>(S.pack)[p] = make_float2(v[0], v[1]);
-    else
+    // images: also transposed, after the row-major copy (see fan_fp_kernel)
+    const int pt = bins ? -1 : npix + (p % n) * n + p / n;
+    if (S.nmem == 2) {
+      float2 *pk = reinterpret_cast<float2 *>(S.pack);
+      pk[p] = make_float2(v[0], v[1]);
+      if (pt >= 0) pk[pt] = make_float2(v[0], v[1]);
+    } else {
       S.pack[p] = make_float4(v[0], v[1], v[2], v[3]);
+      if (pt >= 0) S.pack[pt] = make_float4(v[0], v[1], v[2], v[3]);
+    }
   }
 }
 
@@ -133,6 +142,30 @@ __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
       for (int m = 0; m < G; m++) acc[r][m] = comp[r][m] = 0.f;
       my_max = max(my_max, nseg[r]);
     }
+    // Groups gather from the transposed copy of the interleaved images when the
+    // warp's rays run closer to the y axis: a warp's rays then lie side by side
+    // along x, and in the transposed copy neighbouring x share a sector (the
+    // row-major copy serves rays closer to the x axis).  Blocks with rays off
+    // the grid keep the row-major copy, whose index checks they rely on.
+    const float4 *__restrict__ pk4 = pack;
+    const float2 *__restrict__ pk2 = pack2;
+    if constexpr (G > 1) {
+      const float lx0 = __shfl_sync(0xffffffffu, lx[0], 0), ly0 = __shfl_sync(0xffffffffu, ly[0], 0);
+      if (!__ldg(S.blk_off + blk) && lx0 > ly0) {
+        pk4 += npix;
+        pk2 += npix;
+#pragma unroll
+        for (int r = 0; r < RPT; r++) {
+          if (nseg[r] == 0) continue;
+          const int xy = __ldg(&S.rays[(size_t)view * S.ndets + det0 + r].xy0);
+          const int x0 = xy & 0xffff, y0 = xy >> 16;
+          idx[r] = y0 * S.n + x0;
+          const int sx = stx[r] > 0 ? 1 : -1, sy = sty[r] > 0 ? S.n : -S.n;
+          stx[r] = sx;
+          sty[r] = sy;
+        }
+      }
+    }
     // warp-uniform trip count, and the words that are full for every ray
     int my_min = nseg[0];
 #pragma unroll
@@ -181,11 +214,11 @@ __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
             if constexpr (G == 1) {
               part[r][0] = fmaf(wt, __ldg(img + idx[r]), part[r][0]);
             } else if constexpr (G == 2) {
-              const float2 v = __ldg(pack2 + idx[r]);
+              const float2 v = __ldg(pk2 + idx[r]);
               part[r][0] = fmaf(wt, v.x, part[r][0]);
               part[r][1] = fmaf(wt, v.y, part[r][1]);
             } else {
-              const float4 v = __ldg(pack + idx[r]);
+              const float4 v = __ldg(pk4 + idx[r]);
               part[r][0] = fmaf(wt, v.x, part[r][0]);
               part[r][1] = fmaf(wt, v.y, part[r][1]);
               part[r][2] = fmaf(wt, v.z, part[r][2]);
@@ -214,12 +247,12 @@ __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
               part[r][0] = fmaf(wt, val, part[r][0]);
             } else if constexpr (G == 2) {
               float2 v = make_float2(0.f, 0.f);
-              if (on) v = __ldg(pack2 + idx[r]);
+              if (on) v = __ldg(pk2 + idx[r]);
               part[r][0] = fmaf(wt, v.x, part[r][0]);
               part[r][1] = fmaf(wt, v.y, part[r][1]);
             } else {
               float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-              if (on) v = __ldg(pack + idx[r]);
+              if (on) v = __ldg(pk4 + idx[r]);
               part[r][0] = fmaf(wt, v.x, part[r][0]);
               part[r][1] = fmaf(wt, v.y, part[r][1]);
               part[r][2] = fmaf(wt, v.z, part[r][2]);

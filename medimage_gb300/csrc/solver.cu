@@ -90,7 +90,8 @@ ScanLayout layout_of(const Plan &p, int rpt) {
   L.bp_bytes = bp_scratch_bytes(p);
   // fan beam and ray tables: a group's forward-projector inputs, interleaved
   const bool packs = p.kind == AT_GEOM_FAN || p.kind == AT_GEOM_RAYS;
-  L.pack_bytes = packs ? align_up(sizeof(float4) * std::max((size_t)p.n * p.n, nbins)) : 0;
+  // (images twice: row-major and transposed)
+  L.pack_bytes = packs ? align_up(sizeof(float4) * std::max(2 * (size_t)p.n * p.n, nbins)) : 0;
   L.total = L.img_bytes * B_NIMG + L.sino_bytes * (B_NBUF - B_NIMG) + L.partial_bytes + L.trace_bytes +
             L.bp_bytes + L.pack_bytes + align_up(sizeof(Ctl));
   return L;
@@ -448,7 +449,7 @@ int ProjSet::create(const std::vector<Plan *> &pl) {
   rpt = Solver::choose_rpt(pl);
   const int n = (int)pl.size();
   auto pack_of = [](const Plan &p) {
-    const size_t elems = std::max((size_t)p.n * p.n, (size_t)p.nviews * p.ndets);
+    const size_t elems = std::max(2 * (size_t)p.n * p.n, (size_t)p.nviews * p.ndets);
     return (p.kind == AT_GEOM_FAN || p.kind == AT_GEOM_RAYS) ? align_up(sizeof(float4) * elems) : 0;
   };
   size_t total = 256;

@@ -108,7 +108,7 @@ struct ScanDev {
   unsigned long long *bp_acc;  // [npix]
   int *bp_cnt;                 // [ntiles]
   int bp_split;                // CTAs per tile (>= 1)
-  float4 *pack;                // [max(n*n, nbins)] fan/ray plans: a group's projector inputs, interleaved
+  float4 *pack;                // [max(2*n*n, nbins)] fan/ray plans: a group's projector inputs, interleaved
   // scans of a batch that share this scan's plan and are projected together
   // with it: nmem members (scan indices, this one first) on the lead; 0 on
   // the others, which get no projector CTAs of their own

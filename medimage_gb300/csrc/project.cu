@@ -42,13 +42,13 @@ namespace at {
 // float2 per element for a pair, one float4 for three or four members, zeros
 // for absent or finished members; images twice, row-major and transposed
 // (the forward projector reads whichever puts a warp's neighbouring rays in
-// fewer sectors): images (bins = 0,
+// fewer sectors), and for a scan alone only its image transposed: images (bins = 0,
 // over the pixel-pass CTAs) before a grouped forward projection, sinograms
 // (bins = 1, over the sinogram-pass CTAs) before a grouped back projection.
 __global__ void __launch_bounds__(256) fp_pack_kernel(const Launch L, int bins) {
   const int scan = find_scan(L.prefix, L.nscans, blockIdx.x);
   const ScanDev &S = L.scans[scan];
-  if (S.nmem < 2) return;  // a scan alone is read in place
+  if (S.nmem == 0 || (S.nmem == 1 && bins)) return;  // a scan alone: its sinogram is read in place
   const float *src[kGroupMax];
   bool any = false;
 #pragma unroll
@@ -61,6 +61,12 @@ __global__ void __launch_bounds__(256) fp_pack_kernel(const Launch L, int bins) 
   const int cta0 = __ldg(L.prefix + scan), ncta = __ldg(L.prefix + scan + 1) - cta0;
   const int n = S.n, npix = n * n;
   const int count = bins ? S.nbins : npix;
+  if (S.nmem == 1) {  // a scan alone: only the transposed image, as floats
+    float *t = reinterpret_cast<float *>(S.pack);
+    for (int p = (blockIdx.x - cta0) * blockDim.x + threadIdx.x; p < npix; p += ncta * blockDim.x)
+      t[(p % n) * n + p / n] = src[0] ? __ldg(src[0] + p) : 0.f;
+    return;
+  }
   for (int p = (blockIdx.x - cta0) * blockDim.x + threadIdx.x; p < count; p += ncta * blockDim.x) {
     float v[kGroupMax];
 #pragma unroll
@@ -111,7 +117,7 @@ __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
     const int in_blk = slice * 32 * RPT + lane * RPT;  // first ray of this thread within the block
     const int det0 = (blk % S.nbpv) * kRayBlock + in_blk;
     static_assert(G == 1 || G == 2 || G == 4, "members are gathered as one float, float2 or float4");
-    const float *__restrict__ img = M[0]->buf[L.in_buf];
+    const float *__restrict__ img = M[0]->buf[L.in_buf];  // (or its transposed copy, below)
     const float4 *__restrict__ pack = S.pack;
     const float2 *__restrict__ pack2 = reinterpret_cast<const float2 *>(S.pack);
     const unsigned npix = (unsigned)S.npix;
@@ -142,18 +148,20 @@ __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
       for (int m = 0; m < G; m++) acc[r][m] = comp[r][m] = 0.f;
       my_max = max(my_max, nseg[r]);
     }
-    // Groups gather from the transposed copy of the interleaved images when the
-    // warp's rays run closer to the y axis: a warp's rays then lie side by side
-    // along x, and in the transposed copy neighbouring x share a sector (the
-    // row-major copy serves rays closer to the x axis).  Blocks with rays off
-    // the grid keep the row-major copy, whose index checks they rely on.
+    // With a transposed copy of the inputs (L.tr: the scan's pack buffer), a
+    // warp whose rays run closer to the y axis gathers from it: its rays then
+    // lie side by side along x, and in the transposed copy neighbouring x share
+    // a sector (the row-major copy serves rays closer to the x axis).  Blocks
+    // with rays off the grid keep the row-major copy, whose index checks they
+    // rely on.
     const float4 *__restrict__ pk4 = pack;
     const float2 *__restrict__ pk2 = pack2;
-    if constexpr (G > 1) {
+    if (L.tr) {
       const float lx0 = __shfl_sync(0xffffffffu, lx[0], 0), ly0 = __shfl_sync(0xffffffffu, ly[0], 0);
       if (!__ldg(S.blk_off + blk) && lx0 > ly0) {
         pk4 += npix;
         pk2 += npix;
+        if constexpr (G == 1) img = reinterpret_cast<const float *>(S.pack);
 #pragma unroll
         for (int r = 0; r < RPT; r++) {
           if (nseg[r] == 0) continue;
@@ -773,19 +781,33 @@ int launch_fp_group(const Launch &L, const Launch &Lpix, const Launch &L1, const
                     int nctas1, int nctas2, cudaStream_t st) {
   int n = 1;
   fp_pack_kernel<<<pix_nctas, 256, 0, st>>>(Lpix, 0);
+  Launch Lg = L, Lg1 = L1, Lg2 = L2;
+  Lg.tr = Lg1.tr = Lg2.tr = 1;
   if (nctas > 0) {
-    fan_fp_kernel<1, kGroupMax><<<nctas, kFpGroupThreads, 0, st>>>(L);
+    fan_fp_kernel<1, kGroupMax><<<nctas, kFpGroupThreads, 0, st>>>(Lg);
     n++;
   }
   if (nctas1 > 0) {
-    fan_fp_kernel<1, 1><<<nctas1, kFpGroupThreads, 0, st>>>(L1);
+    fan_fp_kernel<1, 1><<<nctas1, kFpGroupThreads, 0, st>>>(Lg1);
     n++;
   }
   if (nctas2 > 0) {
-    fan_fp_kernel<1, 2><<<nctas2, kFpGroupThreads, 0, st>>>(L2);
+    fan_fp_kernel<1, 2><<<nctas2, kFpGroupThreads, 0, st>>>(Lg2);
     n++;
   }
   return n;
+}
+
+// Forward projection of a batch of fan-beam / ray-table scans without groups:
+// each scan's input transposed into its pack buffer (over the pixel-pass CTAs
+// of Lpix), then the walk with RPT rays per thread.  Returns the number of
+// launches.
+int launch_fp_tr(const Launch &L, const Launch &Lpix, int rpt, int nctas, int pix_nctas, cudaStream_t st) {
+  fp_pack_kernel<<<pix_nctas, 256, 0, st>>>(Lpix, 0);
+  Launch Lt = L;
+  Lt.tr = 1;
+  launch_fp(Lt, AT_GEOM_FAN, rpt, nctas, st);
+  return 2;
 }
 
 // Back projection of a batch whose scans sharing a plan are grouped: the max

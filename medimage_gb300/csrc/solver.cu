@@ -23,6 +23,7 @@ int pix_ctas(const ScanDev &S);
 cudaError_t launch_fp(const Launch &L, int kind, int rpt, int nctas, cudaStream_t st);
 int launch_fp_group(const Launch &L, const Launch &Lpix, const Launch &L1, const Launch &L2, int nctas, int pix_nctas,
                     int nctas1, int nctas2, cudaStream_t st);
+int launch_fp_tr(const Launch &L, const Launch &Lpix, int rpt, int nctas, int pix_nctas, cudaStream_t st);
 int launch_bp_group(const Launch &L, const Launch &Lsino, const Launch &Lsmall, int nctas, int sino_nctas,
                     int small_nctas, cudaStream_t st);
 cudaError_t launch_bp(const Launch &L, int kind, int nctas, cudaStream_t st, const Launch *Lpix, int pix_nctas);
@@ -256,6 +257,11 @@ int Batch::enqueue_fp(const Launch &L, cudaStream_t st) {
     L1.prefix = prefix_d + FAM_FP1 * (nscans + 1);
     L2.prefix = prefix_d + FAM_FP2 * (nscans + 1);
     launches += launch_fp_group(L, Lp, L1, L2, fp_total, pix_total, fp1_total, fp2_total, st);
+    AT_CUDA_TRY(cudaGetLastError());
+  } else if (kind == AT_GEOM_FAN || kind == AT_GEOM_RAYS) {  // transpose each input, then walk
+    Launch Lp = L;
+    Lp.prefix = prefix_d + FAM_PIX * (nscans + 1);
+    launches += launch_fp_tr(L, Lp, rpt, fp_total, pix_total, st);
     AT_CUDA_TRY(cudaGetLastError());
   } else {
     AT_CUDA_TRY(launch_fp(L, kind, rpt, fp_total, st));

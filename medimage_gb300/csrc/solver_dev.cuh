@@ -133,6 +133,7 @@ struct Launch {
   int k;                         // inner iteration this launch belongs to
   int flag;                      // kernel-specific (median this iteration, first pass, ...)
   int group;                     // projector launches: largest group of scans sharing a plan
+  int tr;                        // forward projection: the scans' pack buffers hold transposed inputs
 };
 
 __device__ __forceinline__ int find_scan(const int *prefix, int nscans, int cta) {

@@ -14,6 +14,7 @@
 namespace at {
 
 int fp_ctas(const ScanDev &S, int rpt);
+cudaError_t launch_fp_single_tr(const Launch &L, int rpt, int nctas, float *tr, cudaStream_t st);
 int bp_ctas(const ScanDev &S);
 cudaError_t launch_fp(const Launch &L, int kind, int rpt, int nctas, cudaStream_t st);
 cudaError_t launch_bp(const Launch &L, int kind, int nctas, cudaStream_t st, const Launch *Lpix, int pix_nctas);
@@ -61,7 +62,15 @@ int project(const Plan &p, bool forward, const float *in, float *out, cudaStream
   cudaError_t e;
   if (forward) {
     const int rpt = projector_rpt(p);
-    e = launch_fp(L, p.kind, rpt, fp_ctas(L.single, rpt), st);
+    if (p.kind == AT_GEOM_FAN || p.kind == AT_GEOM_RAYS) {
+      // stream-ordered scratch for the image's transposed copy
+      float *tr = nullptr;
+      AT_CUDA_TRY(cudaMallocAsync(&tr, sizeof(float) * (size_t)p.n * p.n, st));
+      e = launch_fp_single_tr(L, rpt, fp_ctas(L.single, rpt), tr, st);
+      cudaFreeAsync(tr, st);
+    } else {
+      e = launch_fp(L, p.kind, rpt, fp_ctas(L.single, rpt), st);
+    }
   } else {
     // stream-ordered scratch: calls on other streams never share it
     const size_t bpb = bp_scratch_bytes(p);

@@ -798,6 +798,35 @@ int launch_fp_group(const Launch &L, const Launch &Lpix, const Launch &L1, const
   return n;
 }
 
+// out[y][x] = in[x][y] for an n x n image, through 32 x 32 shared-memory tiles
+// (coalesced reads and writes)
+__global__ void __launch_bounds__(256) transpose_kernel(const float *__restrict__ in, float *__restrict__ out,
+                                                         int n) {
+  __shared__ float t[32][33];
+  const int bx = blockIdx.x * 32, by = blockIdx.y * 32;
+  for (int r = threadIdx.y; r < 32; r += 8) {
+    const int x = by + r, y = bx + threadIdx.x;
+    if (x < n && y < n) t[r][threadIdx.x] = in[(size_t)x * n + y];
+  }
+  __syncthreads();
+  for (int r = threadIdx.y; r < 32; r += 8) {
+    const int y = bx + r, x = by + threadIdx.x;
+    if (x < n && y < n) out[(size_t)y * n + x] = t[threadIdx.x][r];
+  }
+}
+
+// One fan-beam / ray-table forward projection outside a batch, reading its
+// image's transposed copy (`tr`, n x n floats of scratch) where the rays run
+// closer to the y axis.
+cudaError_t launch_fp_single_tr(const Launch &L, int rpt, int nctas, float *tr, cudaStream_t st) {
+  const int n = L.single.n;
+  transpose_kernel<<<dim3((n + 31) / 32, (n + 31) / 32), dim3(32, 8), 0, st>>>(L.single.buf[L.in_buf], tr, n);
+  Launch Lt = L;
+  Lt.single.pack = reinterpret_cast<float4 *>(tr);
+  Lt.tr = 1;
+  return launch_fp(Lt, AT_GEOM_FAN, rpt, nctas, st);
+}
+
 // Forward projection of a batch of fan-beam / ray-table scans without groups:
 // each scan's input transposed into its pack buffer (over the pixel-pass CTAs
 // of Lpix), then the walk with RPT rays per thread.  Returns the number of

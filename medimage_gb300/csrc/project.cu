@@ -330,7 +330,7 @@ __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
 constexpr int kBpPitch = kBpTile + 1;  // padded row pitch of the accumulator
 constexpr int kBpAccWords = kBpTile * kBpPitch;
 constexpr int kBpCopies1 = 4;  // copies, single-scan launches (C2: 1 copy 0.33 ms, 4 copies 0.275 ms)
-constexpr int kBpCopiesG = 4;  // copies per member, grouped launches
+constexpr int kBpCopiesG = 8;  // copies per member, grouped launches (four slices: 2 copies 0.90 ms, 4 0.785, 8 0.764)
 template <int C>
 constexpr int bp_copy_stride() {
   return kBpAccWords + ((32 / C - kBpAccWords % 32) % 32 + 32) % 32;

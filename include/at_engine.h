@@ -144,7 +144,10 @@ int at_plan_trace_ray(const at_plan *plan, int32_t view, int32_t det, int32_t *h
                       int32_t cap, int32_t *n_out);
 
 /* ---- projectors (FP32, device buffers) ---- */
-/* d_sino[view][det] = sum over the ray's segments of d_img[pixel] * weight */
+/* d_sino[view][det] = sum over the ray's segments of d_img[pixel] * weight.
+ * Fan beam and ray tables take stream-ordered scratch (cudaMallocAsync) for
+ * the image's transposed copy, which the walk reads where rays run closer to
+ * the y axis; the sums are the same either way. */
 int at_forward(const at_plan *plan, const float *d_img, float *d_sino, void *stream);
 /* d_img = A^T d_sino; deterministic: each pixel is an exact integer sum of
  * fixed-point terms (no float atomics), so the result does not depend on

@@ -111,27 +111,27 @@ __global__ void __launch_bounds__(256) upd_kernel(const Launch L) {
   const float c1 = (float)S.ctl->c1;
   float cp = 0.f;
   for_my_pixels(n, local_cta, [&](const PixCoord &c) {
-    if (!c.inside) return;
-    const float pc = p[c.i];
-    cp = fmaxf(cp, fabsf(c1 * pc));
-    if (!L.flag) {
-      out[c.i] = fmaf(c1, pc, u[c.i]);
-    } else {
-      float w[3][3];
-#pragma unroll
-      for (int dx = -1; dx <= 1; dx++)
-#pragma unroll
-        for (int dy = -1; dy <= 1; dy++) {
-          const int xx = c.x + dx, yy = c.y + dy;
-          float val = 0.f;
-          if (xx >= 0 && xx < n && yy >= 0 && yy < n) {
-            const int j = c.base + xx * n + yy;
-            val = fmaf(c1, p[j], u[j]);
+      if (!c.inside) return;
+      const float pc = p[c.i];
+      cp = fmaxf(cp, fabsf(c1 * pc));
+      if (!L.flag) {
+        out[c.i] = fmaf(c1, pc, u[c.i]);
+      } else {
+        float w[3][3];
+  #pragma unroll
+        for (int dx = -1; dx <= 1; dx++)
+  #pragma unroll
+          for (int dy = -1; dy <= 1; dy++) {
+            const int xx = c.x + dx, yy = c.y + dy;
+            float val = 0.f;
+            if (xx >= 0 && xx < n && yy >= 0 && yy < n) {
+              const int j = c.base + xx * n + yy;
+              val = fmaf(c1, p[j], u[j]);
+            }
+            w[dx + 1][dy + 1] = val;
           }
-          w[dx + 1][dy + 1] = val;
-        }
-      out[c.i] = median9(w[0], w[1], w[2]);
-    }
+        out[c.i] = median9(w[0], w[1], w[2]);
+      }
   });
   cta_max_to_ctl(S, cp);
   reduce_and_finalize<0>(S, L, nullptr, local_cta, ncta);
@@ -188,18 +188,18 @@ __global__ void __launch_bounds__(256) edge_init_kernel(const Launch L) {
   const int n = S.n;
   const float *__restrict__ f = S.buf[B_F];
   for_my_pixels(n, local_cta, [&](const PixCoord &c) {
-  if (!c.inside) return;
-  const float fd = c.x + 1 < n ? f[c.i + n] : 0.f, fu = c.x > 0 ? f[c.i - n] : 0.f;
-  const float fr = c.y + 1 < n ? f[c.i + 1] : 0.f, fl = c.y > 0 ? f[c.i - 1] : 0.f;
-  const float gx = 0.5f * (fd - fu), gy = 0.5f * (fr - fl);
-  if (S.nz == 1) {
-    S.buf[B_NN][c.i] = gx * gx + gy * gy;
-  } else {
-    const int nn = n * n;
-    const float fb = c.z + 1 < S.nz ? f[c.i + nn] : 0.f, ff = c.z > 0 ? f[c.i - nn] : 0.f;
-    const float gz = 0.5f * (fb - ff);
-    S.buf[B_NN][c.i] = gx * gx + gy * gy + gz * gz;
-  }
+    if (!c.inside) return;
+    const float fd = c.x + 1 < n ? f[c.i + n] : 0.f, fu = c.x > 0 ? f[c.i - n] : 0.f;
+    const float fr = c.y + 1 < n ? f[c.i + 1] : 0.f, fl = c.y > 0 ? f[c.i - 1] : 0.f;
+    const float gx = 0.5f * (fd - fu), gy = 0.5f * (fr - fl);
+    if (S.nz == 1) {
+      S.buf[B_NN][c.i] = gx * gx + gy * gy;
+    } else {
+      const int nn = n * n;
+      const float fb = c.z + 1 < S.nz ? f[c.i + nn] : 0.f, ff = c.z > 0 ? f[c.i - nn] : 0.f;
+      const float gz = 0.5f * (fb - ff);
+      S.buf[B_NN][c.i] = gx * gx + gy * gy + gz * gz;
+    }
   });
 }
 
@@ -215,49 +215,49 @@ __global__ void __launch_bounds__(256) edge_d_kernel(const Launch L) {
   const float b4 = (float)(ct->beta / (4 * ct->eps));
   FF sums[3] = {ff_zero(), ff_zero(), ff_zero()};
   for_my_pixels(n, local_cta, [&](const PixCoord &c) {
-  if (c.inside && S.nz == 1) {
-    auto vat = [&](int xx, int yy) -> float {
-      return (xx >= 0 && xx < n && yy >= 0 && yy < n) ? v[xx * n + yy] : 1.f;
-    };
-    auto dat = [&](int xx, int yy) -> float {
-      if (xx < 0 || xx >= n || yy < 0 || yy >= n) return 0.f;
-      const float vc = v[xx * n + yy];
-      const float lap = 0.25f * (vat(xx + 1, yy) + vat(xx, yy + 1) - 4.f * vc + vat(xx - 1, yy) + vat(xx, yy - 1));
-      const float g = alpha * vc * nn[xx * n + yy] - beq * lap + b4 * (vc - 1.f);
-      return -g;
-    };
-    const float dc = dat(c.x, c.y);
-    S.buf[B_D][c.i] = dc;
-    // non-negative terms, rounded in FP32 (d^2 exactly)
-    ff_acc(sums[0], ff_prod(dc, dc));
-    ff_acc(sums[1], ff_of(nn[c.i] * (dc * dc)));
-    const float gx = 0.5f * (dat(c.x + 1, c.y) - dat(c.x - 1, c.y));
-    const float gy = 0.5f * (dat(c.x, c.y + 1) - dat(c.x, c.y - 1));
-    ff_acc(sums[2], ff_of(fmaf(gx, gx, gy * gy)));
-  } else if (c.inside) {
-    // volumes: six-neighbour Laplacian scaled by 1/6, central differences in z
-    const int nz = S.nz;
-    auto vat = [&](int zz, int xx, int yy) -> float {
-      return (zz >= 0 && zz < nz && xx >= 0 && xx < n && yy >= 0 && yy < n) ? v[(zz * n + xx) * n + yy] : 1.f;
-    };
-    auto dat = [&](int zz, int xx, int yy) -> float {
-      if (zz < 0 || zz >= nz || xx < 0 || xx >= n || yy < 0 || yy >= n) return 0.f;
-      const int j = (zz * n + xx) * n + yy;
-      const float vc = v[j];
-      const float lap = (1.f / 6.f) * (vat(zz, xx + 1, yy) + vat(zz, xx, yy + 1) + vat(zz + 1, xx, yy) - 6.f * vc +
-                                      vat(zz, xx - 1, yy) + vat(zz, xx, yy - 1) + vat(zz - 1, xx, yy));
-      const float g = alpha * vc * nn[j] - beq * lap + b4 * (vc - 1.f);
-      return -g;
-    };
-    const float dc = dat(c.z, c.x, c.y);
-    S.buf[B_D][c.i] = dc;
-    ff_acc(sums[0], ff_prod(dc, dc));
-    ff_acc(sums[1], ff_of(nn[c.i] * (dc * dc)));
-    const float gx = 0.5f * (dat(c.z, c.x + 1, c.y) - dat(c.z, c.x - 1, c.y));
-    const float gy = 0.5f * (dat(c.z, c.x, c.y + 1) - dat(c.z, c.x, c.y - 1));
-    const float gz = 0.5f * (dat(c.z + 1, c.x, c.y) - dat(c.z - 1, c.x, c.y));
-    ff_acc(sums[2], ff_of(fmaf(gx, gx, fmaf(gy, gy, gz * gz))));
-  }
+    if (c.inside && S.nz == 1) {
+      auto vat = [&](int xx, int yy) -> float {
+        return (xx >= 0 && xx < n && yy >= 0 && yy < n) ? v[xx * n + yy] : 1.f;
+      };
+      auto dat = [&](int xx, int yy) -> float {
+        if (xx < 0 || xx >= n || yy < 0 || yy >= n) return 0.f;
+        const float vc = v[xx * n + yy];
+        const float lap = 0.25f * (vat(xx + 1, yy) + vat(xx, yy + 1) - 4.f * vc + vat(xx - 1, yy) + vat(xx, yy - 1));
+        const float g = alpha * vc * nn[xx * n + yy] - beq * lap + b4 * (vc - 1.f);
+        return -g;
+      };
+      const float dc = dat(c.x, c.y);
+      S.buf[B_D][c.i] = dc;
+      // non-negative terms, rounded in FP32 (d^2 exactly)
+      ff_acc(sums[0], ff_prod(dc, dc));
+      ff_acc(sums[1], ff_of(nn[c.i] * (dc * dc)));
+      const float gx = 0.5f * (dat(c.x + 1, c.y) - dat(c.x - 1, c.y));
+      const float gy = 0.5f * (dat(c.x, c.y + 1) - dat(c.x, c.y - 1));
+      ff_acc(sums[2], ff_of(fmaf(gx, gx, gy * gy)));
+    } else if (c.inside) {
+      // volumes: six-neighbour Laplacian scaled by 1/6, central differences in z
+      const int nz = S.nz;
+      auto vat = [&](int zz, int xx, int yy) -> float {
+        return (zz >= 0 && zz < nz && xx >= 0 && xx < n && yy >= 0 && yy < n) ? v[(zz * n + xx) * n + yy] : 1.f;
+      };
+      auto dat = [&](int zz, int xx, int yy) -> float {
+        if (zz < 0 || zz >= nz || xx < 0 || xx >= n || yy < 0 || yy >= n) return 0.f;
+        const int j = (zz * n + xx) * n + yy;
+        const float vc = v[j];
+        const float lap = (1.f / 6.f) * (vat(zz, xx + 1, yy) + vat(zz, xx, yy + 1) + vat(zz + 1, xx, yy) - 6.f * vc +
+                                        vat(zz, xx - 1, yy) + vat(zz, xx, yy - 1) + vat(zz - 1, xx, yy));
+        const float g = alpha * vc * nn[j] - beq * lap + b4 * (vc - 1.f);
+        return -g;
+      };
+      const float dc = dat(c.z, c.x, c.y);
+      S.buf[B_D][c.i] = dc;
+      ff_acc(sums[0], ff_prod(dc, dc));
+      ff_acc(sums[1], ff_of(nn[c.i] * (dc * dc)));
+      const float gx = 0.5f * (dat(c.z, c.x + 1, c.y) - dat(c.z, c.x - 1, c.y));
+      const float gy = 0.5f * (dat(c.z, c.x, c.y + 1) - dat(c.z, c.x, c.y - 1));
+      const float gz = 0.5f * (dat(c.z + 1, c.x, c.y) - dat(c.z - 1, c.x, c.y));
+      ff_acc(sums[2], ff_of(fmaf(gx, gx, fmaf(gy, gy, gz * gz))));
+    }
   });
   reduce_and_finalize<3>(S, L, sums, local_cta, ncta);
 }

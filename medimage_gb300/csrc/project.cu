@@ -30,13 +30,20 @@ namespace at {
 // ---------------------------------------------------------------------------
 // fan-beam forward projection
 // ---------------------------------------------------------------------------
+// A thread walks its ray by the plan's decision bits and gathers one pixel
+// per segment.  The 32 rays of a warp are neighbours in one view, so at a
+// given step they lie side by side across the ray direction: a warp whose
+// rays run closer to the y axis reads a transposed copy of the image (made
+// just before the walk), where its pixels share sectors.
+//
 // A batch's scans that share one plan form a group (up to kGroupMax, listed in
 // the lead scan's ScanDev).  Their input images are first interleaved into the
-// lead's pack buffer (fp_pack_kernel, one float4 per pixel); the lead's CTAs
-// then walk each ray once and one 16-byte gather per segment feeds every
-// member, so the walk (decision bits, crossing arithmetic) and the gathers are
-// shared.  Each member's sum is formed exactly as it would be alone, so
-// results do not depend on the grouping.
+// lead's pack buffer (fp_pack_kernel, one float4 per pixel, row-major and
+// transposed); the lead's CTAs then walk each ray once and one 16-byte gather
+// per segment feeds every member, so the walk (decision bits, crossing
+// arithmetic) and the gathers are shared.  Each member's sum is formed exactly
+// as it would be alone, so results do not depend on the grouping or on the
+// copy a warp reads.
 
 // Interleaves each group's projector inputs into the lead's pack buffer, one
 // float2 per element for a pair, one float4 for three or four members, zeros
@@ -316,13 +323,14 @@ __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
 // overflow 32 bits) and added to a shared-memory 32-bit accumulator; after
 // each view block every thread folds its pixel into an exact 64-bit register
 // sum.  A tile's view blocks may be split over several CTAs (load balance when
-// a launch has few tiles); their 64-bit sums add exactly in global memory.  Integer addition is associative, so the result does not depend on the
-// order in which lanes, warps or views arrive (deterministic, no float
-// atomics).  Scans of a batch that share the plan are back-projected together
-// (up to kGroupMax, listed in the lead scan): each run is loaded and walked
-// once and its weights go to every member's accumulator, each with the
-// member's own residual and scale, so each member's integer sum is exactly the
-// one it gets alone.
+// a launch has few tiles); their 64-bit sums add exactly in global memory.
+// Integer addition is associative, so the result does not depend on the order
+// in which lanes, warps or views arrive (deterministic, no float atomics).
+// Scans of a batch that share the plan are back-projected together (up to
+// kGroupMax, listed in the lead scan; their residuals interleaved by
+// fp_pack_kernel): each run is loaded and walked once and its weights go to
+// every member's accumulator, each with the member's own residual and scale,
+// so each member's integer sum is exactly the one it gets alone.
 // Lanes of a warp that add to the same pixel in one instruction serialise, and
 // a warp's runs (similar lengths through one tile, from nearby views) often
 // meet: each member therefore keeps C accumulator copies, lane l adding to copy

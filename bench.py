@@ -738,7 +738,7 @@ def run_reference(args):
     ph = ellipse_phantom(spec.geom.n, seed=spec.seed, n_random=spec.n_random)
     clean = po.fan_A(fan, ph.astype(np.float64), cores)
     sino = poisson_sinogram(clean, spec.i0, spec.seed + 1000).astype(np.float64)
-    for _ in range(args.warmup and 1):
+    for _ in range(args.warmup):
         po.solve(fan, sino, 1000.0, 0.002, 1e-4, 1, 10, 10, nthreads=cores)
     t0 = time.perf_counter()
     for _ in range(args.steps):

@@ -77,7 +77,10 @@ int project(const Plan &p, bool forward, const float *in, float *out, cudaStream
     void *scratch = nullptr;
     if (bpb) {
       AT_CUDA_TRY(cudaMallocAsync(&scratch, bpb, st));
-      AT_CUDA_TRY(cudaMemsetAsync(scratch, 0, bpb, st));
+      if ((e = cudaMemsetAsync(scratch, 0, bpb, st)) != cudaSuccess) {
+        cudaFreeAsync(scratch, st);
+        return cuda_error(e, "back projection scratch");
+      }
       carve_bp_scratch(L.single, p, (char *)scratch);
       L.single.bp_split = bp_split_for(p.ntiles, p.nvb);
     }
@@ -612,7 +615,13 @@ AT_API void A(double proj[180][767], double orig[512][512]) {
   int rc = C.init();
   if (!rc) rc = C.to_dev(&orig[0][0], C.fa, kGcPix);
   float *sino = nullptr;
-  if (!rc && cudaMallocAsync(&sino, sizeof(float) * kGcBins, C.st) != cudaSuccess) rc = cuda_error(cudaGetLastError(), "cudaMallocAsync");
+  if (!rc) {
+    const cudaError_t e = cudaMallocAsync(&sino, sizeof(float) * kGcBins, C.st);
+    if (e != cudaSuccess) {
+      sino = nullptr;
+      rc = cuda_error(e, "cudaMallocAsync");
+    }
+  }
   if (!rc) rc = project(C.plan->p, true, C.fa, sino, C.st);
   if (!rc) rc = C.to_host(sino, &proj[0][0], kGcBins);
   if (sino) {
@@ -627,7 +636,13 @@ AT_API void AStar(double back[512][512], double proj[180][767]) {
   std::lock_guard<std::mutex> lk(C.mu);
   int rc = C.init();
   float *sino = nullptr;
-  if (!rc && cudaMallocAsync(&sino, sizeof(float) * kGcBins, C.st) != cudaSuccess) rc = cuda_error(cudaGetLastError(), "cudaMallocAsync");
+  if (!rc) {
+    const cudaError_t e = cudaMallocAsync(&sino, sizeof(float) * kGcBins, C.st);
+    if (e != cudaSuccess) {
+      sino = nullptr;
+      rc = cuda_error(e, "cudaMallocAsync");
+    }
+  }
   if (!rc) rc = C.to_dev(&proj[0][0], sino, kGcBins);
   if (!rc) rc = project(C.plan->p, false, sino, C.fa, C.st);
   if (!rc) rc = C.to_host(C.fa, &back[0][0], kGcPix);

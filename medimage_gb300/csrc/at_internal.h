@@ -97,6 +97,20 @@ int cuda_error(cudaError_t e, const char *what);
     if (_e != cudaSuccess) return ::at::cuda_error(_e, #expr); \
   } while (0)
 
+// Runs f when the enclosing scope ends, on every return path: a function's
+// device temporaries are released when an AT_CUDA_TRY returns early as well
+// as on success.  cudaFree(nullptr) does nothing, so temporaries not yet
+// allocated are harmless.
+template <typename F>
+struct ScopeExit {
+  F f;
+  ~ScopeExit() { f(); }
+};
+template <typename F>
+ScopeExit<F> scope_exit(F f) {
+  return ScopeExit<F>{f};
+}
+
 // host-side geometry tables with the reference's libm expressions
 void fan_tables(const at_fan_geometry &g, double *scos, double *ssin, double *dcos, double *dsin);
 int validate_fan(const at_fan_geometry &g);

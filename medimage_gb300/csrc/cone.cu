@@ -425,6 +425,7 @@ int build_cone_plan(Plan &p, cudaStream_t st) {
   ScanDev S;
   fill_scan_plan(S, p);
   unsigned long long *cnt = nullptr;
+  const auto free_cnt = scope_exit([&] { cudaFree(cnt); });
   AT_CUDA_TRY(cudaMalloc(&cnt, 3 * sizeof(unsigned long long)));
   AT_CUDA_TRY(cudaMemsetAsync(cnt, 0, 3 * sizeof(unsigned long long), st));
   cone_count_kernel<<<(unsigned)((p.rays + 255) / 256), 256, 0, st>>>(S, cnt, cnt + 1, (int *)(cnt + 2));
@@ -432,7 +433,6 @@ int build_cone_plan(Plan &p, cudaStream_t st) {
   unsigned long long h[3];
   AT_CUDA_TRY(cudaMemcpyAsync(h, cnt, sizeof(h), cudaMemcpyDeviceToHost, st));
   AT_CUDA_TRY(cudaStreamSynchronize(st));
-  cudaFree(cnt);
   p.segments = (int64_t)h[0];
   p.offgrid = (int64_t)h[1];
   p.max_segments = (int)(unsigned)(h[2] & 0xffffffffu);
@@ -445,6 +445,11 @@ int cone_trace_ray(const Plan &p, int64_t ray, int32_t *h_pix, float *h_w, int32
   const int dcap = std::max(cap, 1);
   int *pix = nullptr, *cnt = nullptr;
   float *wgt = nullptr;
+  const auto free_temps = scope_exit([&] {
+    cudaFree(pix);
+    cudaFree(wgt);
+    cudaFree(cnt);
+  });
   AT_CUDA_TRY(cudaMalloc(&pix, sizeof(int) * dcap));
   AT_CUDA_TRY(cudaMalloc(&wgt, sizeof(float) * dcap));
   AT_CUDA_TRY(cudaMalloc(&cnt, sizeof(int)));
@@ -455,9 +460,6 @@ int cone_trace_ray(const Plan &p, int64_t ray, int32_t *h_pix, float *h_w, int32
   const int m = std::min(n, cap);
   if (m > 0 && h_pix) AT_CUDA_TRY(cudaMemcpy(h_pix, pix, sizeof(int) * m, cudaMemcpyDeviceToHost));
   if (m > 0 && h_w) AT_CUDA_TRY(cudaMemcpy(h_w, wgt, sizeof(float) * m, cudaMemcpyDeviceToHost));
-  cudaFree(pix);
-  cudaFree(wgt);
-  cudaFree(cnt);
   *n_out = n;
   return AT_OK;
 }

@@ -102,6 +102,10 @@ AT_API int at_psnr(const float *d_x, const float *d_ref, int64_t n, double peak,
   cudaStream_t st = (cudaStream_t)stream;
   double *psum = nullptr;
   unsigned *pmax = nullptr;
+  const auto free_temps = scope_exit([&] {
+    if (psum) cudaFreeAsync(psum, st);
+    if (pmax) cudaFreeAsync(pmax, st);
+  });
   AT_CUDA_TRY(cudaMallocAsync(&psum, sizeof(double) * kBlocks, st));
   AT_CUDA_TRY(cudaMallocAsync(&pmax, sizeof(unsigned) * kBlocks, st));
   psnr_partial_kernel<<<kBlocks, kThreads, 0, st>>>(d_x, d_ref, n, psum, pmax);
@@ -110,8 +114,6 @@ AT_API int at_psnr(const float *d_x, const float *d_ref, int64_t n, double peak,
   unsigned hm[kBlocks];
   AT_CUDA_TRY(cudaMemcpyAsync(hs, psum, sizeof(hs), cudaMemcpyDeviceToHost, st));
   AT_CUDA_TRY(cudaMemcpyAsync(hm, pmax, sizeof(hm), cudaMemcpyDeviceToHost, st));
-  AT_CUDA_TRY(cudaFreeAsync(psum, st));
-  AT_CUDA_TRY(cudaFreeAsync(pmax, st));
   AT_CUDA_TRY(cudaStreamSynchronize(st));
   double s = 0.0;
   unsigned m = 0u;
@@ -155,12 +157,14 @@ AT_API int at_ssim(const float *d_x, const float *d_ref, int32_t h, int32_t w, d
   const double c1 = (0.01 * dynamic_range) * (0.01 * dynamic_range);
   const double c2 = (0.03 * dynamic_range) * (0.03 * dynamic_range);
   double *part = nullptr;
+  const auto free_part = scope_exit([&] {
+    if (part) cudaFreeAsync(part, st);
+  });
   AT_CUDA_TRY(cudaMallocAsync(&part, sizeof(double) * kBlocks, st));
   ssim_partial_kernel<<<kBlocks, kThreads, 0, st>>>(d_x, d_ref, h, w, c1, c2, part);
   AT_CUDA_TRY(cudaGetLastError());
   double hp[kBlocks];
   AT_CUDA_TRY(cudaMemcpyAsync(hp, part, sizeof(hp), cudaMemcpyDeviceToHost, st));
-  AT_CUDA_TRY(cudaFreeAsync(part, st));
   AT_CUDA_TRY(cudaStreamSynchronize(st));
   double s = 0.0;
   for (double v : hp) s += v;

@@ -297,6 +297,21 @@ int build_fan_runs(Plan &p, cudaStream_t st) {
   const size_t ncell = (size_t)p.ntiles * p.nvb;
   int *cnt_d = nullptr;
   unsigned long long *cur_d = nullptr;
+  uint4 *tmp_ent = nullptr;
+  unsigned long long *keys = nullptr, *keys_out = nullptr;
+  unsigned *idx = nullptr, *idx_out = nullptr, *hits = nullptr;
+  void *temp = nullptr;
+  const auto free_temps = scope_exit([&] {
+    cudaFree(hits);
+    cudaFree(temp);
+    cudaFree(tmp_ent);
+    cudaFree(keys);
+    cudaFree(keys_out);
+    cudaFree(idx);
+    cudaFree(idx_out);
+    cudaFree(cnt_d);
+    cudaFree(cur_d);
+  });
   AT_CUDA_TRY(cudaMalloc(&cnt_d, sizeof(int) * ncell));
   AT_CUDA_TRY(cudaMalloc(&cur_d, sizeof(unsigned long long)));
   AT_CUDA_TRY(cudaMemsetAsync(cnt_d, 0, sizeof(int) * ncell, st));
@@ -317,9 +332,6 @@ int build_fan_runs(Plan &p, cudaStream_t st) {
   if (tot >= (1ll << 31)) return set_error(AT_EINVAL, "plan: too many back-projection runs");
   off[ncell] = (int32_t)tot;
   p.nruns = tot;
-  uint4 *tmp_ent = nullptr;
-  unsigned long long *keys = nullptr, *keys_out = nullptr;
-  unsigned *idx = nullptr, *idx_out = nullptr;
   AT_CUDA_TRY(cudaMalloc(&tmp_ent, sizeof(uint4) * std::max<int64_t>(tot, 1)));
   AT_CUDA_TRY(cudaMalloc(&keys, sizeof(unsigned long long) * std::max<int64_t>(tot, 1)));
   AT_CUDA_TRY(cudaMalloc(&keys_out, sizeof(unsigned long long) * std::max<int64_t>(tot, 1)));
@@ -334,7 +346,6 @@ int build_fan_runs(Plan &p, cudaStream_t st) {
   // keys are unique (tile, view block, 63-nk, view, det): the sorted order is deterministic
   size_t temp_bytes = 0;
   AT_CUDA_TRY(cub::DeviceRadixSort::SortPairs(nullptr, temp_bytes, keys, keys_out, idx, idx_out, (int64_t)tot, 0, 64, st));
-  void *temp = nullptr;
   AT_CUDA_TRY(cudaMalloc(&temp, std::max<size_t>(temp_bytes, 1)));
   AT_CUDA_TRY(cub::DeviceRadixSort::SortPairs(temp, temp_bytes, keys, keys_out, idx, idx_out, (int64_t)tot, 0, 64, st));
   int rc;
@@ -357,7 +368,7 @@ int build_fan_runs(Plan &p, cudaStream_t st) {
     per_block = (double)per_view * kBpViewBlock;
   } else {
     const size_t cells = (size_t)p.n * p.n;
-    unsigned *hits = nullptr, *mx = nullptr;
+    unsigned *mx = nullptr;
     AT_CUDA_TRY(cudaMalloc(&hits, sizeof(unsigned) * (cells + 1)));
     mx = hits + cells;
     AT_CUDA_TRY(cudaMemsetAsync(mx, 0, sizeof(unsigned), st));
@@ -373,21 +384,12 @@ int build_fan_runs(Plan &p, cudaStream_t st) {
     unsigned m = 0;
     AT_CUDA_TRY(cudaMemcpyAsync(&m, mx, sizeof(m), cudaMemcpyDeviceToHost, st));
     AT_CUDA_TRY(cudaStreamSynchronize(st));
-    cudaFree(hits);
     per_block = std::max(1u, m);
   }
   // terms stay below 2^22 so the kernel can round them with one FFMA
   p.bp_term_bits = std::min(22, 31 - (int)std::ceil(std::log2(per_block + 1.0)));
   if (p.bp_term_bits < 16) return set_error(AT_EINVAL, "plan: detector far finer than the pixel grid (back projector precision)");
   AT_CUDA_TRY(cudaStreamSynchronize(st));
-  cudaFree(temp);
-  cudaFree(tmp_ent);
-  cudaFree(keys);
-  cudaFree(keys_out);
-  cudaFree(idx);
-  cudaFree(idx_out);
-  cudaFree(cnt_d);
-  cudaFree(cur_d);
   return AT_OK;
 }
 

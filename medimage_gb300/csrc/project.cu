@@ -896,6 +896,13 @@ int autotune_fan(Plan &p, cudaStream_t st) {
   p.fp_rpt = 1;
   if (p.kind == AT_GEOM_GOLDNC || p.kind == AT_GEOM_CONE) return AT_OK;
   float *img = nullptr, *sino = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  const auto free_temps = scope_exit([&] {
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (img) cudaFreeAsync(img, st);
+    if (sino) cudaFreeAsync(sino, st);
+  });
   const size_t npix = (size_t)p.n * p.n, nbins = (size_t)p.nviews * p.ndets;
   AT_CUDA_TRY(cudaMallocAsync(&img, npix * sizeof(float), st));
   AT_CUDA_TRY(cudaMallocAsync(&sino, nbins * sizeof(float), st));
@@ -911,7 +918,6 @@ int autotune_fan(Plan &p, cudaStream_t st) {
   L.in_buf = 0;
   L.out_buf = 1;
   L.aux_buf = -1;
-  cudaEvent_t e0, e1;
   AT_CUDA_TRY(cudaEventCreate(&e0));
   AT_CUDA_TRY(cudaEventCreate(&e1));
   float best = 1e30f;
@@ -929,10 +935,6 @@ int autotune_fan(Plan &p, cudaStream_t st) {
       p.fp_rpt = rpt;
     }
   }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  cudaFreeAsync(img, st);
-  cudaFreeAsync(sino, st);
   AT_CUDA_TRY(cudaStreamSynchronize(st));
   return AT_OK;
 }

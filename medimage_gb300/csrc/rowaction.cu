@@ -388,12 +388,12 @@ AT_API int at_rowaction_create(int32_t n, int32_t nproj, int32_t nray, at_rowact
   AT_CUDA_TRY(cudaMalloc(&R->trig, sizeof(float2) * nproj));
   AT_CUDA_TRY(cudaMemcpy(R->trig, trig.data(), sizeof(float2) * nproj, cudaMemcpyHostToDevice));
   int *cnt = nullptr;
+  const auto free_cnt = scope_exit([&] { cudaFree(cnt); });
   AT_CUDA_TRY(cudaMalloc(&cnt, sizeof(int) * rays));
   ra_count_kernel<<<(rays + 127) / 128, 128>>>(R->G, R->trig, cnt);
   AT_CUDA_TRY(cudaGetLastError());
   std::vector<int> h(rays);
   AT_CUDA_TRY(cudaMemcpy(h.data(), cnt, sizeof(int) * rays, cudaMemcpyDeviceToHost));
-  cudaFree(cnt);
   std::vector<int64_t> off(rays + 1, 0);
   for (int r = 0; r < rays; r++) {
     if (h[r] > kRaMaxSeg) return set_error(AT_EINVAL, "at_rowaction_create: a ray crosses more than 2048 pixels");

@@ -423,14 +423,16 @@ class Plan:
 
     def forward(self, img: np.ndarray) -> np.ndarray:
         img = np.ascontiguousarray(img, np.float32)
-        assert img.shape == self.img_shape
+        if img.shape != self.img_shape:
+            raise ValueError(f"image shape {img.shape}, plan expects {self.img_shape}")
         out = np.zeros(self.sino_shape, np.float32)
         _check("at_forward_host", lib().at_forward_host(self._h, img, out))
         return out
 
     def back(self, sino: np.ndarray) -> np.ndarray:
         sino = np.ascontiguousarray(sino, np.float32)
-        assert sino.shape == self.sino_shape
+        if sino.shape != self.sino_shape:
+            raise ValueError(f"sinogram shape {sino.shape}, plan expects {self.sino_shape}")
         out = np.zeros(self.img_shape, np.float32)
         _check("at_back_host", lib().at_back_host(self._h, sino, out))
         return out
@@ -470,7 +472,8 @@ class ProjSet:
             pass
 
     def _ptrs(self, ptrs):
-        assert len(ptrs) == len(self.plans)
+        if len(ptrs) != len(self.plans):
+            raise ValueError(f"{len(ptrs)} pointers for {len(self.plans)} plans")
         return (C.c_void_p * len(ptrs))(*[C.c_void_p(p) for p in ptrs])
 
     def forward_dev(self, d_imgs, d_sinos, stream: int = 0) -> None:
@@ -518,7 +521,8 @@ class Solver:
     def set_sino(self, scan: int, sino: np.ndarray, stream: int = 0) -> None:
         p = self.plans[scan]
         sino = np.ascontiguousarray(sino, np.float32)
-        assert sino.shape == p.sino_shape
+        if sino.shape != p.sino_shape:
+            raise ValueError(f"sinogram shape {sino.shape}, scan {scan}'s plan expects {p.sino_shape}")
         self._keep = sino  # host buffer must live until the copy completes
         _check("at_solver_set_sino_host", lib().at_solver_set_sino_host(self._h, scan, sino, C.c_void_p(stream)))
         self.sync(stream)
@@ -740,7 +744,8 @@ def quality(x: np.ndarray, ref: np.ndarray, peak: float = 0.0, dynamic_range: fl
     """PSNR (peak <= 0: max(ref)) and SSIM computed on the GPU (at_psnr, at_ssim)."""
     x = np.ascontiguousarray(x, np.float32)
     ref = np.ascontiguousarray(ref, np.float32)
-    assert x.shape == ref.shape and x.ndim == 2
+    if x.shape != ref.shape or x.ndim != 2:
+        raise ValueError(f"quality: shapes {x.shape} and {ref.shape}; two equal 2D images are needed")
     L = lib()
     ptrs = []
     try:

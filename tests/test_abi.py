@@ -57,6 +57,13 @@ def test_bad_geometry_rejected_without_device(engine):
         engine.Plan.fan(g)
 
 
+def test_quality_rejects_mismatched_images_without_device(engine):
+    with pytest.raises(ValueError):
+        engine.quality(np.zeros((16, 16), np.float32), np.zeros((16, 17), np.float32))
+    with pytest.raises(ValueError):
+        engine.quality(np.zeros(16, np.float32), np.zeros(16, np.float32))
+
+
 def test_bad_ray_table_rejected_without_device(engine):
     g = engine.RayGeometry.msbeam_parallel(64, 8, 96)
     bad = g.endpoints.copy()

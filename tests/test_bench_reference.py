@@ -3,7 +3,11 @@ restatement of origin/GoldenC/src/main.c with the fan tracer) timed on the
 host cores, printing the same metric, unit and config as the GPU arm.
 
 Under torchrun only rank 0 runs it; every other rank exits 0 without work and
-prints nothing."""
+prints nothing.
+
+Also the GPU arm's GoldenC side sample (GoldenC at its own geometry beside the
+drop-in entry points), driven here by an oracle-backed stand-in library: its
+fields, and an error field rather than an exception when the library fails."""
 import json
 import os
 import subprocess
@@ -45,3 +49,44 @@ def test_reference_arm_other_ranks_do_no_work():
     p = _run({"RANK": "1", "WORLD_SIZE": "2", "LOCAL_RANK": "1"})
     assert p.returncode == 0, p.stderr[-2000:]
     assert p.stdout.strip() == ""
+
+
+class _OracleDropin:
+    """GoldenC's drop-in entry points answered by the FP64 oracle, so that the
+    bench's GoldenC sample can be exercised without a GPU."""
+
+    def __init__(self, oracle):
+        self.o = oracle
+
+    def A(self, proj, img):
+        proj[...] = self.o.gc_A(img)
+
+    def minimize_in_IMAGE_variable(self, out, g, f, v, alpha, epsilon, it):
+        out[...] = self.o.image_step(None, g, f, v, alpha, epsilon, it)[0]
+
+    def minimize_in_EDGE_variable(self, out, f, v, alpha, beta, epsilon, it):
+        out[...] = self.o.edge_step(f, v, alpha, beta, epsilon, it)[0]
+
+    def goldnc_status(self):
+        return 0
+
+
+def test_goldnc_sample_fields_and_errors(oracle):
+    import types
+
+    sys.path.insert(0, ROOT)
+    import bench
+    import medimage_gb300.phantom as phantom
+
+    mg = types.SimpleNamespace(lib=lambda: _OracleDropin(oracle), phantom=phantom)
+    out = bench.run_goldnc_native(mg, reps=1)
+    assert "error" not in out, out
+    assert out["goldnc_cpu"] == {"cores": 1, "kind": "port"}
+    assert out["engine_dropin_s"] > 0 and out["goldnc_cpu_s"] > 0 and out["status"] == 0
+    assert out["rel_l2_f"] == 0.0 and out["rel_l2_v"] == 0.0  # the stand-in is the oracle itself
+
+    def broken():
+        raise OSError("library missing")
+
+    bad = bench.run_goldnc_native(types.SimpleNamespace(lib=broken, phantom=phantom), reps=1)
+    assert bad == {"error": "OSError: library missing"}

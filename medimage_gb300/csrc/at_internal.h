@@ -23,7 +23,7 @@
 
 #include "../../include/at_engine.h"
 
-namespace at {
+namespace medimg {
 
 constexpr int kRayBlock = 128;  // rays per decision-bit block (one view)
 constexpr int kBpTile = 16;     // back-projection tile edge (pixels)
@@ -94,7 +94,7 @@ int cuda_error(cudaError_t e, const char *what);
 #define AT_CUDA_TRY(expr)                                   \
   do {                                                      \
     cudaError_t _e = (expr);                                \
-    if (_e != cudaSuccess) return ::at::cuda_error(_e, #expr); \
+    if (_e != cudaSuccess) return ::medimg::cuda_error(_e, #expr); \
   } while (0)
 
 // Runs f when the enclosing scope ends, on every return path: a function's
@@ -125,8 +125,8 @@ int validate_rays(int n, double pixel_mm, int nviews, int ndets, const double *h
 int build_goldnc_plan(Plan &p, cudaStream_t st);
 int autotune_fan(Plan &p, cudaStream_t st);
 
-}  // namespace at
+}  // namespace medimg
 
 struct at_plan {
-  at::Plan p;
+  medimg::Plan p;
 };

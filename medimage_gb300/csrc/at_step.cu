@@ -15,7 +15,7 @@
 
 #include "solver_dev.cuh"
 
-namespace at {
+namespace medimg {
 
 struct PixCoord {
   int x, y, z, i, base;  // base: index of the slice's first pixel
@@ -352,9 +352,9 @@ cudaError_t launch_flags(const ScanDev *scans, int nscans, int mode, cudaStream_
   return cudaGetLastError();
 }
 
-}  // namespace at
+}  // namespace medimg
 
-namespace at {
+namespace medimg {
 
 // Standalone 3x3 median with zero padding (main.c:366-390), out of place.
 __global__ void __launch_bounds__(256) median_kernel(const float *__restrict__ in, float *__restrict__ out, int n) {
@@ -378,9 +378,9 @@ cudaError_t launch_median(const float *in, float *out, int n, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-}  // namespace at
+}  // namespace medimg
 
-namespace at {
+namespace medimg {
 
 __global__ void fill_kernel(float *p, float v, size_t n) {
   const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
@@ -392,4 +392,4 @@ cudaError_t launch_fill(float *p, float v, size_t n, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-}  // namespace at
+}  // namespace medimg

@@ -11,7 +11,7 @@
 #include "../../include/goldnc.h"
 #include "solver.h"
 
-namespace at {
+namespace medimg {
 
 int fp_ctas(const ScanDev &S, int rpt);
 cudaError_t launch_fp_single_tr(const Launch &L, int rpt, int nctas, float *tr, cudaStream_t st);
@@ -101,9 +101,9 @@ __global__ void f2d_kernel(const float *in, double *out, int64_t n) {
 }
 
 }  // namespace
-}  // namespace at
+}  // namespace medimg
 
-using namespace at;
+using namespace medimg;
 
 #define AT_API extern "C" __attribute__((visibility("default")))
 #define AT_CHECK_ARG(cond, msg) \
@@ -538,14 +538,34 @@ struct GoldncContext {
   float *fa = nullptr, *fb = nullptr;
   int iter_alt = 10, iter_image = 10, iter_edge = 10;
   int status = AT_OK;
+  // Creates the stream, the staging buffers and then the plan.  `plan` is set
+  // last, so a context is either complete or still empty: a failure part way
+  // frees what was made and the next call starts over.
   int init() {
     if (plan) return AT_OK;
-    int rc = at_plan_create_goldnc(&plan);
-    if (rc) return rc;
-    AT_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-    AT_CUDA_TRY(cudaMalloc(&dd, sizeof(double) * kGcPix));
-    AT_CUDA_TRY(cudaMalloc(&fa, sizeof(float) * kGcPix));
-    AT_CUDA_TRY(cudaMalloc(&fb, sizeof(float) * kGcPix));
+    cudaStream_t s = nullptr;
+    double *d = nullptr;
+    float *a = nullptr, *b = nullptr;
+    at_plan *p = nullptr;
+    int rc = AT_OK;
+    cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&d, sizeof(double) * kGcPix);
+    if (e == cudaSuccess) e = cudaMalloc(&a, sizeof(float) * kGcPix);
+    if (e == cudaSuccess) e = cudaMalloc(&b, sizeof(float) * kGcPix);
+    if (e != cudaSuccess) rc = cuda_error(e, "GoldenC context set-up");
+    if (!rc) rc = at_plan_create_goldnc(&p);
+    if (rc) {
+      cudaFree(d);
+      cudaFree(a);
+      cudaFree(b);
+      if (s) cudaStreamDestroy(s);
+      return rc;
+    }
+    st = s;
+    dd = d;
+    fa = a;
+    fb = b;
+    plan = p;
     return AT_OK;
   }
   int to_dev(const double *h, float *d, int n) {
@@ -693,10 +713,15 @@ AT_API void MumfordShah(double alpha, double beta, double epsilon) {
     std::vector<Plan *> pl{&C.plan->p};
     Solver S;
     if (!(rc = S.create(pl, prm))) {
+      // f and v are written together, after both have reached the host: a
+      // failure leaves the program's globals as they were
       const ScanDev &D = S.host_scans[0];
+      std::vector<double> hf(kGcPix), hv(kGcPix);
       if (!(rc = C.to_dev(&gDelta[0][0], D.buf[B_G], kGcBins)) && !(rc = S.run(C.st)) &&
-          !(rc = C.to_host(D.buf[B_F], &f[0][0], kGcPix)))
-        rc = C.to_host(D.buf[B_V], &v[0][0], kGcPix);
+          !(rc = C.to_host(D.buf[B_F], hf.data(), kGcPix)) && !(rc = C.to_host(D.buf[B_V], hv.data(), kGcPix))) {
+        std::memcpy(&f[0][0], hf.data(), sizeof(double) * kGcPix);
+        std::memcpy(&v[0][0], hv.data(), sizeof(double) * kGcPix);
+      }
     }
   }
   goldnc_report("MumfordShah", rc);

@@ -23,7 +23,7 @@
 #include "epilogue.cuh"
 #include "solver.h"
 
-namespace at {
+namespace medimg {
 
 // State of one ray's walk (tracing.cpp:131-265).
 struct ConeWalk {
@@ -464,4 +464,4 @@ int cone_trace_ray(const Plan &p, int64_t ray, int32_t *h_pix, float *h_w, int32
   return AT_OK;
 }
 
-}  // namespace at
+}  // namespace medimg

@@ -4,7 +4,7 @@
 
 #include "solver_dev.cuh"
 
-namespace at {
+namespace medimg {
 
 // ---------------------------------------------------------------------------
 // epilogues
@@ -106,4 +106,4 @@ __device__ __forceinline__ void kahan_add(float &sum, float &comp, float x) {
   sum = t;
 }
 
-}  // namespace at
+}  // namespace medimg

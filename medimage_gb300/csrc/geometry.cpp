@@ -8,7 +8,7 @@
 
 #include "at_internal.h"
 
-namespace at {
+namespace medimg {
 
 // helical/rebin/src/ms2d.cpp:43-54: source angle table (degrees -> cos/sin)
 // and the equiangular detector table with OFF_CENTER.
@@ -89,4 +89,4 @@ int validate_cone(const at_cone_geometry &g) {
   return AT_OK;
 }
 
-}  // namespace at
+}  // namespace medimg

@@ -14,7 +14,7 @@
 
 #include "at_internal.h"
 
-namespace at {
+namespace medimg {
 namespace {
 
 constexpr int kWin = 11;
@@ -91,9 +91,9 @@ __global__ void ssim_partial_kernel(const float *x, const float *y, int h, int w
 constexpr int kBlocks = 512, kThreads = 256;
 
 }  // namespace
-}  // namespace at
+}  // namespace medimg
 
-using namespace at;
+using namespace medimg;
 
 #define AT_API extern "C" __attribute__((visibility("default")))
 

@@ -25,7 +25,7 @@
 
 #include "solver.h"
 
-namespace at {
+namespace medimg {
 
 int fp_ctas(const ScanDev &S, int rpt);
 cudaError_t launch_fp(const Launch &L, int kind, int rpt, int nctas, cudaStream_t st);
@@ -58,9 +58,9 @@ int scratch_address(void **out) {
 }
 
 }  // namespace
-}  // namespace at
+}  // namespace medimg
 
-using namespace at;
+using namespace medimg;
 
 extern "C" __attribute__((visibility("default"))) int at_forward_residual_noalloc(const at_plan *plan,
                                                                                    const float *d_img,

@@ -17,7 +17,7 @@
 
 #include "at_internal.h"
 
-namespace at {
+namespace medimg {
 
 // ---------------------------------------------------------------------------
 // fan beam
@@ -717,4 +717,4 @@ Plan::~Plan() {
   cudaFree(cone_trig_d);
 }
 
-}  // namespace at
+}  // namespace medimg

@@ -24,7 +24,7 @@
 #include "epilogue.cuh"
 #include "solver.h"
 
-namespace at {
+namespace medimg {
 
 
 // ---------------------------------------------------------------------------
@@ -886,9 +886,9 @@ cudaError_t launch_bp(const Launch &L, int kind, int nctas, cudaStream_t st, con
   return cudaGetLastError();
 }
 
-}  // namespace at
+}  // namespace medimg
 
-namespace at {
+namespace medimg {
 
 // Times the forward projector with 1, 2 and 4 rays per thread on this plan and
 // keeps the fastest (results are bitwise identical across the three).
@@ -939,4 +939,4 @@ int autotune_fan(Plan &p, cudaStream_t st) {
   return AT_OK;
 }
 
-}  // namespace at
+}  // namespace medimg

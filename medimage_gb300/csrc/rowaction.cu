@@ -25,7 +25,7 @@
 
 #include "at_internal.h"
 
-namespace at {
+namespace medimg {
 namespace {
 
 struct RaGeom {
@@ -286,7 +286,7 @@ __global__ void ra_init_kernel(float *f, float *v, size_t n) {
 }
 
 }  // namespace
-}  // namespace at
+}  // namespace medimg
 
 // A run is one launch per (sweep, view, phase), a few microseconds of work
 // each, so it is captured as a CUDA graph and replayed; the graph is kept for
@@ -306,7 +306,7 @@ struct RaGraphKey {
 };
 
 struct at_rowaction {
-  at::RaGeom G{};
+  medimg::RaGeom G{};
   float2 *trig = nullptr;
   int64_t *off = nullptr;
   int *line = nullptr;
@@ -330,7 +330,7 @@ struct at_rowaction {
   }
 };
 
-using namespace at;
+using namespace medimg;
 
 namespace {
 // msbeam's run (main.c:365-394): f = 0, v = 1, then `sweeps` sweeps of every

@@ -25,7 +25,7 @@
 
 #include "solver.h"
 
-namespace at {
+namespace medimg {
 
 cudaError_t launch_fill(float *p, float v, size_t n, cudaStream_t st);
 
@@ -234,13 +234,13 @@ struct Server {
   }
 };
 
-}  // namespace at
+}  // namespace medimg
 
 struct at_server {
-  at::Server s;
+  medimg::Server s;
 };
 
-using namespace at;
+using namespace medimg;
 
 #define AT_API extern "C" __attribute__((visibility("default")))
 

@@ -14,7 +14,7 @@
 
 #include "solver.h"
 
-namespace at {
+namespace medimg {
 
 int fp_ctas(const ScanDev &S, int rpt);
 int fp_group_ctas(const ScanDev &S);
@@ -574,4 +574,4 @@ int Solver::run(cudaStream_t st) {
   return step(params.iter_alt, st);
 }
 
-}  // namespace at
+}  // namespace medimg

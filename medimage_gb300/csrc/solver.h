@@ -6,7 +6,7 @@
 
 #include "solver_dev.cuh"
 
-namespace at {
+namespace medimg {
 
 void fill_scan_plan(ScanDev &S, const Plan &p);
 // device bytes of one scan's state (images, sinograms, partials, trace, control)
@@ -102,12 +102,12 @@ struct ProjSet {
   ~ProjSet();
 };
 
-}  // namespace at
+}  // namespace medimg
 
 struct at_projset {
-  at::ProjSet p;
+  medimg::ProjSet p;
 };
 
 struct at_solver {
-  at::Solver s;
+  medimg::Solver s;
 };

@@ -14,7 +14,7 @@
 
 #include "at_internal.h"
 
-namespace at {
+namespace medimg {
 
 // image-shaped buffers, then sinogram-shaped buffers
 enum Buf : int {
@@ -444,4 +444,4 @@ __device__ __forceinline__ void atomic_max_nonneg(unsigned *addr, float x) {
   atomicMax(addr, __float_as_uint(x));
 }
 
-}  // namespace at
+}  // namespace medimg

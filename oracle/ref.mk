@@ -2,13 +2,15 @@
 # read-only reference tree, into oracle/_ref/ (git-ignored).  Used only to pin
 # the oracle restatement and to generate golden vectors.
 #
-#   make -f oracle/ref.mk REF=/root/reference
+#   make -f oracle/ref.mk REF=<path of the reference tree>
 #
 # Flags: -O2 without -ffast-math and with -ffp-contract=off, matching
 # oracle/Makefile, so that FP64 results can be compared bit for bit.  (The
 # reference's own Makefiles add -march=native -ffast-math, which lets the
 # compiler reassociate; those binaries are used for timing only.)
-REF ?= /root/reference
+ifndef REF
+$(error REF=<path of the reference tree> is required)
+endif
 HERE := $(dir $(abspath $(lastword $(MAKEFILE_LIST))))
 OUT := $(HERE)_ref
 CC ?= gcc

@@ -2,7 +2,7 @@
 sources (compiled by oracle/ref.mk into oracle/_ref/).  Run where the reference
 tree is present:
 
-    make -f oracle/ref.mk REF=/root/reference && python tests/golden/make_golden.py
+    make -f oracle/ref.mk REF=<reference tree> && python tests/golden/make_golden.py
 
 Fixtures (all inputs are seeded and regenerated by the tests):
   goldnc.npz  GoldenC proj.c A / AStar outputs (checksums + crops), sparse

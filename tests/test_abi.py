@@ -12,7 +12,8 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 INCLUDE = os.path.join(ROOT, "include")
-REF_GOLDNC = "/root/reference/origin/GoldenC/src"
+REF_ROOT = os.environ.get("MEDIMAGE_REFERENCE") or os.path.join(os.path.dirname(ROOT), "reference")
+REF_GOLDNC = os.path.join(REF_ROOT, "origin", "GoldenC", "src")
 
 
 def declared_functions():

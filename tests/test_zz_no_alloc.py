@@ -33,31 +33,46 @@ def _host(L, engine, dptr, shape, dtype):
     return out
 
 
-@pytest.mark.parametrize("kind", ["fan", "goldnc"])
+def _plan(engine, kind):
+    if kind == "fan":
+        return engine.Plan.fan(engine.FanGeometry.covering(256, 1.0, 360, 512))
+    if kind == "rays":  # a non-uniform view table, given ray by ray
+        ang = np.sort(np.random.default_rng(5).uniform(0.0, 360.0, 150))
+        return engine.Plan.rays(engine.RayGeometry.fan_from_view_table(128, 1.0, 200, ang, det_pitch_deg=0.19))
+    if kind == "cone":
+        return engine.Plan.cone(engine.ConeGeometry(32, 32, 24, 1.0, 40, 28, 36, 1.6, 80.0, 150.0))
+    return engine.Plan.goldnc()
+
+
+def _image(engine, plan, seed):
+    if len(plan.img_shape) == 3:
+        nz, n, _ = plan.img_shape
+        return engine.phantom.csg_phantom(n, nz, seed=seed, n_parts=4, n_voids=3)
+    return engine.phantom.ellipse_phantom(plan.img_shape[0], seed=seed, n_random=5)
+
+
+@pytest.mark.parametrize("kind", ["fan", "rays", "cone", "goldnc"])
 def test_noalloc_forward_residual_matches_forward(engine, kind):
     L = engine.lib()
-    if kind == "fan":
-        plan = engine.Plan.fan(engine.FanGeometry.covering(256, 1.0, 360, 512))
-    else:
-        plan = engine.Plan.goldnc()
-    n, nv, nd = plan.n, plan.nviews, plan.ndets
+    plan = _plan(engine, kind)
+    shape = plan.sino_shape
     rng = np.random.default_rng(77)
     bufs = []
     for call in range(2):
-        img = engine.phantom.ellipse_phantom(n, seed=50 + call, n_random=5)
-        g = (rng.random((nv, nd)) * 4.0).astype(np.float32)
+        img = _image(engine, plan, 50 + call)
+        g = (rng.random(shape) * 4.0).astype(np.float32)
         d_img, d_g = _dev(L, engine, img), _dev(L, engine, g)
-        d_r, d_e = _dev(L, engine, np.zeros((nv, nd), np.float32)), _dev(L, engine, np.zeros(1))
+        d_r, d_e = _dev(L, engine, np.zeros(shape, np.float32)), _dev(L, engine, np.zeros(1))
         bufs += [d_img, d_g, d_r, d_e]
         rc = L.at_forward_residual_noalloc(plan.handle, d_img, d_g, d_r, d_e, None)
         assert rc == 0, L.at_last_error().decode()
-        r = _host(L, engine, d_r, (nv, nd), np.float32)
+        r = _host(L, engine, d_r, shape, np.float32)
         energy = float(_host(L, engine, d_e, (1,), np.float64)[0])
         # the existing entry point
-        d_s = _dev(L, engine, np.zeros((nv, nd), np.float32))
+        d_s = _dev(L, engine, np.zeros(shape, np.float32))
         bufs.append(d_s)
         engine.engine._check("at_forward", L.at_forward(plan.handle, d_img, d_s, None))
-        a = _host(L, engine, d_s, (nv, nd), np.float32)
+        a = _host(L, engine, d_s, shape, np.float32)
         np.testing.assert_array_equal(r, g - a)
         ref = float(np.sum(r.astype(np.float64) ** 2))
         assert abs(energy - ref) <= 1e-12 * ref
@@ -68,7 +83,14 @@ def test_noalloc_forward_residual_matches_forward(engine, kind):
 def test_noalloc_rejects_plans_beyond_its_scratch(engine):
     L = engine.lib()
     plan = engine.Plan.fan(engine.FanGeometry.covering(16, 1.0, 4096, 4096))
-    z = C.c_void_p(16)  # never dereferenced: the size check comes first
-    rc = L.at_forward_residual_noalloc(plan.handle, z, z, z, z, None)
+    # real buffers of the plan's sizes, so that no call can ever reach a
+    # kernel with an invalid address; the size check rejects the call first
+    img = np.zeros(plan.img_shape, np.float32)
+    sino = np.zeros(plan.sino_shape, np.float32)
+    bufs = [_dev(L, engine, img), _dev(L, engine, sino), _dev(L, engine, sino), _dev(L, engine, np.zeros(1))]
+    rc = L.at_forward_residual_noalloc(plan.handle, *bufs, None)
     assert rc == -1
     assert "scratch" in L.at_last_error().decode()
+    np.testing.assert_array_equal(_host(L, engine, bufs[2], plan.sino_shape, np.float32), sino)
+    for p in bufs:
+        L.at_dev_free(p)

@@ -122,6 +122,17 @@ int at_device_info(char *name, int name_len, int *sm_count, size_t *hbm_bytes);
 
 /* ---- plans ---- */
 int at_plan_create_fan(const at_fan_geometry *geom, at_plan **out);
+/* at_plan_create_fan with a choice of traversal arithmetic.  AT_ALPHA_FP64 is
+ * the reference's: forward_proj's lambda entry/exit, start pixel and crossing
+ * merge in double (helical/rebin/src/tracing.cpp:39-146), so the traversed
+ * pixel sequence is the reference's bit for bit; at_plan_create_fan uses it.
+ * AT_ALPHA_FP32 runs the same steps in single precision throughout (the plain
+ * form): no FP64 anywhere on the GPU, and the traversal may depart from the
+ * reference's where two crossings nearly tie.  Kept to measure the precision
+ * of each form against an FP64 oracle. */
+#define AT_ALPHA_FP64 0
+#define AT_ALPHA_FP32 1
+int at_plan_create_fan_ex(const at_fan_geometry *geom, int32_t alpha_precision, at_plan **out);
 int at_plan_create_goldnc(at_plan **out);
 /* 3D cone beam, traced on the fly with the reference's FP32 walk
  * (industry3d/src/tracing.cpp:123-307); nothing per ray is stored. */

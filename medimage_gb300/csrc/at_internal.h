@@ -63,6 +63,7 @@ struct Plan {
   int64_t rays = 0, segments = 0, offgrid = 0, device_bytes = 0;
   int max_segments = 0;
   int fp_rpt = 1;  // rays per thread of the forward projector (autotuned)
+  int alpha_fp32 = 0;  // fan / ray plans traced in FP32 (the plain form) instead of FP64
   // fan
   RayHdr *rays_d = nullptr;
   uint32_t *bits_d = nullptr;

@@ -128,14 +128,17 @@ AT_API int at_device_info(char *name, int name_len, int *sm_count, size_t *hbm_b
 }
 
 // ---------------------------------------------------------------- plans
-AT_API int at_plan_create_fan(const at_fan_geometry *geom, at_plan **out) {
+AT_API int at_plan_create_fan_ex(const at_fan_geometry *geom, int32_t alpha_precision, at_plan **out) {
   AT_CHECK_ARG(geom && out, "at_plan_create_fan: null argument");
+  AT_CHECK_ARG(alpha_precision == AT_ALPHA_FP64 || alpha_precision == AT_ALPHA_FP32,
+               "at_plan_create_fan_ex: alpha_precision must be AT_ALPHA_FP64 or AT_ALPHA_FP32");
   *out = nullptr;
   int rc = validate_fan(*geom);
   if (rc) return rc;
   auto P = std::make_unique<at_plan>();
   P->p.kind = AT_GEOM_FAN;
   P->p.geom = *geom;
+  P->p.alpha_fp32 = alpha_precision == AT_ALPHA_FP32;
   cudaStream_t st;
   AT_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
   rc = build_fan_plan(P->p, st);
@@ -145,6 +148,10 @@ AT_API int at_plan_create_fan(const at_fan_geometry *geom, at_plan **out) {
   if (rc) return rc;
   *out = P.release();
   return AT_OK;
+}
+
+AT_API int at_plan_create_fan(const at_fan_geometry *geom, at_plan **out) {
+  return at_plan_create_fan_ex(geom, AT_ALPHA_FP64, out);
 }
 
 AT_API int at_plan_create_rays(int32_t n, double pixel_mm, int32_t nviews, int32_t ndets, const double *h_endpoints,

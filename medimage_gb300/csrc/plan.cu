@@ -36,56 +36,63 @@ struct RaySource {
   const double *ends;  // [rays][4] for AT_GEOM_RAYS, else null
 };
 
-__device__ __forceinline__ void ray_endpoints(const RaySource &R, int view, int det, double &sx, double &sy,
-                                              double &dx, double &dy) {
+// Real = double: the reference's FP64 arithmetic (bit-identical traversal).
+// Real = float: the same steps in FP32 throughout (tables, end points, lambda
+// entry/exit, start pixel, crossing merge): the plain form, used to measure
+// what the FP64 traversal buys.
+template <typename Real>
+__device__ __forceinline__ void ray_endpoints(const RaySource &R, int view, int det, Real &sx, Real &sy, Real &dx,
+                                              Real &dy) {
   if (R.ends) {
     const double *e = R.ends + ((size_t)view * R.g.ndets + det) * 4;
-    sx = e[0];
-    sy = e[1];
-    dx = e[2];
-    dy = e[3];
+    sx = (Real)e[0];
+    sy = (Real)e[1];
+    dx = (Real)e[2];
+    dy = (Real)e[3];
     return;
   }
   const at_fan_geometry &g = R.g;
-  const double vx = g.pixel_mm, vy = g.pixel_mm;
+  const Real vx = (Real)g.pixel_mm, vy = (Real)g.pixel_mm;
+  const Real sod = (Real)g.sod_mm, sdd = (Real)g.sdd_mm, two = (Real)2.0;
   // ms2d.cpp:172-183
-  const double scos = R.T.scos[view], ssin = R.T.ssin[view];
-  const double dcos = R.T.dcos[det], dsin = R.T.dsin[det];
-  sx = g.sod_mm * scos + g.n * vx / 2.0;
-  sy = g.sod_mm * ssin + g.n * vy / 2.0;
-  dx = g.sdd_mm * (dcos * scos - dsin * ssin) + sx;
-  dy = g.sdd_mm * (dsin * scos + dcos * ssin) + sy;
+  const Real scos = (Real)R.T.scos[view], ssin = (Real)R.T.ssin[view];
+  const Real dcos = (Real)R.T.dcos[det], dsin = (Real)R.T.dsin[det];
+  sx = sod * scos + (Real)g.n * vx / two;
+  sy = sod * ssin + (Real)g.n * vy / two;
+  dx = sdd * (dcos * scos - dsin * ssin) + sx;
+  dy = sdd * (dsin * scos + dcos * ssin) + sy;
 }
 
 // Traces ray (view, det).  Mode 0: fill the header and count segments.
 // Mode 1: also write the decision words into the block-interleaved array.
-template <int kMode>
+template <int kMode, typename Real>
 __device__ void fan_trace_ray(const RaySource &R, int view, int det, RayHdr *hdr, int *offgrid, uint32_t *bits,
                               uint32_t word_stride) {
   const int NX = R.g.n, NY = R.g.n;
-  const double vx = R.g.pixel_mm, vy = R.g.pixel_mm;
-  double sx, sy, dx, dy;
-  ray_endpoints(R, view, det, sx, sy, dx, dy);
+  const Real vx = (Real)R.g.pixel_mm, vy = (Real)R.g.pixel_mm;
+  const Real zero = (Real)0.0, tiny = (Real)1.e-4, huge = (Real)1.e6;
+  Real sx, sy, dx, dy;
+  ray_endpoints<Real>(R, view, det, sx, sy, dx, dy);
   // tracing.cpp:39-87
   int index = 0;
-  const double ray_x = dx - sx, ray_y = dy - sy;
-  const double L = sqrt(ray_x * ray_x + ray_y * ray_y);
-  double lambda_min = 0.0, lambda_max = L;
-  const int signx = (ray_x > 0) ? 1 : -1;
-  const int signy = (ray_y > 0) ? 1 : -1;
-  const double absx = fabs(ray_x), absy = fabs(ray_y);
-  const double len_x = (absx > 1.e-4) ? (L / absx) * vx : 1.e6;
-  const double len_y = (absy > 1.e-4) ? (L / absy) * vy : 1.e6;
-  double tempx = NX * vx, tempy = NY * vy;
-  double l0, lN, temp;
-  l0 = (L * (0.0 - sx)) / (dx - sx);
+  const Real ray_x = dx - sx, ray_y = dy - sy;
+  const Real L = sqrt(ray_x * ray_x + ray_y * ray_y);
+  Real lambda_min = zero, lambda_max = L;
+  const int signx = (ray_x > zero) ? 1 : -1;
+  const int signy = (ray_y > zero) ? 1 : -1;
+  const Real absx = fabs(ray_x), absy = fabs(ray_y);
+  const Real len_x = (absx > tiny) ? (L / absx) * vx : huge;
+  const Real len_y = (absy > tiny) ? (L / absy) * vy : huge;
+  Real tempx = (Real)NX * vx, tempy = (Real)NY * vy;
+  Real l0, lN, temp;
+  l0 = (L * (zero - sx)) / (dx - sx);
   lN = (L * (tempx - sx)) / (dx - sx);
   temp = (l0 < lN) ? l0 : lN;
   lambda_min = (lambda_min > temp) ? lambda_min : temp;
   if (lambda_min == temp) index = 1;
   temp = (l0 > lN) ? l0 : lN;
   lambda_max = (lambda_max < temp) ? lambda_max : temp;
-  l0 = (L * (0.0 - sy)) / (dy - sy);
+  l0 = (L * (zero - sy)) / (dy - sy);
   lN = (L * (tempy - sy)) / (dy - sy);
   temp = (l0 < lN) ? l0 : lN;
   lambda_min = (lambda_min > temp) ? lambda_min : temp;
@@ -108,20 +115,20 @@ __device__ void fan_trace_ray(const RaySource &R, int view, int det, RayHdr *hdr
     }
     return;
   }
-  double lambda0 = lambda_min, lambda_x, lambda_y;
+  Real lambda0 = lambda_min, lambda_x, lambda_y;
   int v_x, v_y;
   if (index == 1) {  // tracing.cpp:91-102
     v_x = (signx == 1) ? 0 : NX - 1;
     lambda_x = lambda0 + len_x;
     v_y = (int)((sy + lambda0 * ray_y / L) / vy);
-    tempy = v_y * vy;
-    lambda_y = (absy < 1.e-4) ? 1.e6 : (L * ((tempy + (signy > 0) * vy) - sy)) / (dy - sy);
+    tempy = (Real)v_y * vy;
+    lambda_y = (absy < tiny) ? huge : (L * ((tempy + (Real)(signy > 0) * vy) - sy)) / (dy - sy);
   } else {  // tracing.cpp:104-115
     v_y = (signy == 1) ? 0 : NY - 1;
     lambda_y = lambda0 + len_y;
     v_x = (int)((sx + lambda0 * ray_x / L) / vx);
-    tempx = v_x * vx;
-    lambda_x = (absx < 1.e-4) ? 1.e6 : (L * ((tempx + (signx > 0) * vx) - sx)) / (dx - sx);
+    tempx = (Real)v_x * vx;
+    lambda_x = (absx < tiny) ? huge : (L * ((tempx + (Real)(signx > 0) * vx) - sx)) / (dx - sx);
   }
   h.pix0 = v_x * NY + v_y;
   h.xy0 = (v_x & 0xffff) | (v_y << 16);
@@ -129,7 +136,7 @@ __device__ void fan_trace_ray(const RaySource &R, int view, int det, RayHdr *hdr
   h.ay = (float)(lambda_y - lambda_min);
   int numb = 0, bad = 0;
   uint32_t word = 0;
-  const double stop = lambda_max - 5.e-2;
+  const Real stop = lambda_max - (Real)5.e-2;
   while (lambda0 < stop) {  // tracing.cpp:118-146
     if ((unsigned)v_x >= (unsigned)NX || (unsigned)v_y >= (unsigned)NY) bad++;
     const bool xstep = lambda_x <= lambda_y;
@@ -159,20 +166,22 @@ __device__ void fan_trace_ray(const RaySource &R, int view, int det, RayHdr *hdr
   }
 }
 
+template <typename Real>
 __global__ void fan_count_kernel(const RaySource R, RayHdr *hdr, int *offgrid) {
   const int ray = blockIdx.x * blockDim.x + threadIdx.x;
   if (ray >= R.g.nviews * R.g.ndets) return;
   const int view = ray / R.g.ndets, det = ray % R.g.ndets;
-  fan_trace_ray<0>(R, view, det, hdr + ray, offgrid + ray, nullptr, 0);
+  fan_trace_ray<0, Real>(R, view, det, hdr + ray, offgrid + ray, nullptr, 0);
 }
 
+template <typename Real>
 __global__ void fan_fill_kernel(const RaySource R, int nblocks_per_view, const uint32_t *blk_word, uint32_t *bits) {
   const int ray = blockIdx.x * blockDim.x + threadIdx.x;
   if (ray >= R.g.nviews * R.g.ndets) return;
   const int view = ray / R.g.ndets, det = ray % R.g.ndets;
   const int blk = view * nblocks_per_view + det / kRayBlock;
   uint32_t *dst = bits + blk_word[blk] + (det % kRayBlock);
-  fan_trace_ray<1>(R, view, det, nullptr, nullptr, dst, kRayBlock);
+  fan_trace_ray<1, Real>(R, view, det, nullptr, nullptr, dst, kRayBlock);
 }
 
 // Segments each pixel receives from each block of kBpViewBlock views, for the
@@ -424,7 +433,10 @@ int build_fan_plan(Plan &p, cudaStream_t st, const double *h_ends) {
   int *off_d = nullptr;
   AT_CUDA_TRY(cudaMalloc(&off_d, sizeof(int) * nrays));
   const int tpb = 128;
-  fan_count_kernel<<<(nrays + tpb - 1) / tpb, tpb, 0, st>>>(R, p.rays_d, off_d);
+  if (p.alpha_fp32)
+    fan_count_kernel<float><<<(nrays + tpb - 1) / tpb, tpb, 0, st>>>(R, p.rays_d, off_d);
+  else
+    fan_count_kernel<double><<<(nrays + tpb - 1) / tpb, tpb, 0, st>>>(R, p.rays_d, off_d);
   AT_CUDA_TRY(cudaGetLastError());
 
   std::vector<RayHdr> hdr(nrays);
@@ -474,7 +486,10 @@ int build_fan_plan(Plan &p, cudaStream_t st, const double *h_ends) {
   AT_CUDA_TRY(cudaMemcpyAsync(p.blk_word_d, blk_word.data(), sizeof(uint32_t) * (p.nblocks + 1),
                               cudaMemcpyHostToDevice, st));
   AT_CUDA_TRY(cudaMemcpyAsync(p.blk_off_d, blk_off.data(), p.nblocks, cudaMemcpyHostToDevice, st));
-  fan_fill_kernel<<<(nrays + tpb - 1) / tpb, tpb, 0, st>>>(R, p.nblocks_per_view, p.blk_word_d, p.bits_d);
+  if (p.alpha_fp32)
+    fan_fill_kernel<float><<<(nrays + tpb - 1) / tpb, tpb, 0, st>>>(R, p.nblocks_per_view, p.blk_word_d, p.bits_d);
+  else
+    fan_fill_kernel<double><<<(nrays + tpb - 1) / tpb, tpb, 0, st>>>(R, p.nblocks_per_view, p.blk_word_d, p.bits_d);
   AT_CUDA_TRY(cudaGetLastError());
 
   if ((rc = build_fan_runs(p, st))) return rc;

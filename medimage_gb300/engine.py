@@ -114,6 +114,7 @@ SIGNATURES = {
     "at_last_error": ([], C.c_char_p),
     "at_device_info": ([C.c_char_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_size_t)], C.c_int),
     "at_plan_create_fan": ([C.POINTER(_FanGeom), C.POINTER(C.c_void_p)], C.c_int),
+    "at_plan_create_fan_ex": ([C.POINTER(_FanGeom), C.c_int32, C.POINTER(C.c_void_p)], C.c_int),
     "at_plan_create_goldnc": ([C.POINTER(C.c_void_p)], C.c_int),
     "at_rowaction_create": ([C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)], C.c_int),
     "at_rowaction_destroy": ([C.c_void_p], None),
@@ -372,10 +373,16 @@ class Plan:
             self.sino_shape = (st.nviews, st.ndets)
 
     @classmethod
-    def fan(cls, geom: FanGeometry) -> "Plan":
+    def fan(cls, geom: FanGeometry, alpha: str = "fp64") -> "Plan":
+        """alpha="fp64": the reference's FP64 traversal (bit-identical pixel
+        sequences); "fp32": the same steps in FP32 (the plain form, kept to
+        measure the precision each form reaches)."""
+        if alpha not in ("fp64", "fp32"):
+            raise ValueError(f"alpha must be 'fp64' or 'fp32', not {alpha!r}")
         h = C.c_void_p()
         g = geom.c()
-        _check("at_plan_create_fan", lib().at_plan_create_fan(C.byref(g), C.byref(h)))
+        _check("at_plan_create_fan_ex", lib().at_plan_create_fan_ex(C.byref(g), 0 if alpha == "fp64" else 1,
+                                                                    C.byref(h)))
         return cls(h, geom)
 
     @classmethod

@@ -13,6 +13,8 @@ import os
 import subprocess
 import sys
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
@@ -90,3 +92,39 @@ def test_goldnc_sample_fields_and_errors(oracle):
 
     bad = bench.run_goldnc_native(types.SimpleNamespace(lib=broken, phantom=phantom), reps=1)
     assert bad == {"error": "OSError: library missing"}
+
+
+def test_parity_block_fields(oracle):
+    """bench.py's C2 parity block, assembled on a small slice with the oracle
+    standing in for both engine forms (so every rel-L2 is 0 up to the order of
+    the oracle's own OpenMP sums, and every exit trace agrees): the background FP64 solve, the fields, the units."""
+    import types
+
+    sys.path.insert(0, ROOT)
+    import bench
+    import medimage_gb300.phantom as phantom
+    from medimage_gb300 import configs
+    from medimage_gb300.engine import FanGeometry
+
+    spec = configs.SliceSpec(FanGeometry.covering(48, 2.0, 60, 80), 1e4, 5, 2, 2)
+    fan = oracle.fan_from_engine(spec.geom)
+    ph = phantom.ellipse_phantom(48, seed=5, n_random=2)
+    sino = phantom.poisson_sinogram(oracle.fan_A(fan, ph.astype(np.float64)), 1e4, 6)
+    ora = bench.OracleSolve(spec, sino, 2)
+    fo, vo, tr = oracle.solve(fan, sino.astype(np.float64), 1000.0, 0.002, 1e-4, 2, 10, 10)
+    trace = [(o, s, k, e, ()) for (o, s, k, _, e) in tr]
+    form = {"fp": oracle.fan_A(fan, ph.astype(np.float64)), "bp": oracle.fan_AT(fan, sino.astype(np.float64)),
+            "f": fo, "v": vo, "trace": trace, "segments": oracle.fan_segments(fan)}
+    mg = types.SimpleNamespace(phantom=phantom)
+    out = bench.finish_parity(mg, spec, {"fp64_alpha": form, "fp32_alpha": form}, ora, ph, sino)
+    assert "error" not in out, out
+    assert out["oracle_solve_s"] > 0 and out["oracle_threads"] == 2
+    assert out["segments_fp64_oracle"] == form["segments"]
+    for name in ("fp64_alpha", "fp32_alpha"):
+        ent = out[name]
+        assert ent["forward_rel_l2"] == 0.0 and ent["back_rel_l2"] == 0.0
+        # the background solve runs on 2 threads, the stand-in's on all:
+        # OpenMP reductions in another order
+        assert ent["f_rel_l2"] <= 1e-12 and ent["v_rel_l2"] <= 1e-12
+        assert abs(ent["psnr_minus_fp64_db"]) <= 1e-3 and ent["exit_branches_identical"] is True
+    json.dumps(out)

@@ -115,6 +115,11 @@ typedef struct at_plan_stats {
     int32_t fp_rays_per_thread; /* forward-projector variant the autotuner chose */
     int64_t bp_runs;       /* (ray, 16x16 tile) runs the back projector walks   */
     int32_t nz;            /* image slices (1 for 2D plans)                      */
+    /* forward projector through shared-memory slabs (fan / ray plans), when the
+     * autotuner chose it over the L1 walk: CTA shape (views x adjacent
+     * detectors), rows per slab, staged columns per slab, and the CTAs that
+     * gather through L1 because a ray leaves the grid; all 0 otherwise */
+    int32_t slab_views, slab_rays, slab_rows, slab_wbox, slab_fallback_ctas;
 } at_plan_stats;
 
 const char *at_last_error(void);
@@ -145,6 +150,19 @@ int at_plan_create_cone(const at_cone_geometry *geom, at_plan **out);
  * (msbeam/CPU_OpenMP/src/proj.c:53-65).  The table is copied. */
 int at_plan_create_rays(int32_t n, double pixel_mm, int32_t nviews, int32_t ndets, const double *h_endpoints,
                         at_plan **out);
+/* Pins the forward projector of a fan-beam or ray-table plan, in place of the
+ * autotuner's choice (results are bitwise the same for every variant):
+ * views = rays = rows = 0 selects the walk that gathers through L1;
+ * otherwise the slab projector with CTAs of `views` consecutive views x
+ * `rays` adjacent detectors (rays divides 128, views * rays <= 512) and slabs
+ * of `rows` image rows.  AT_EINVAL if the shape does not fit this plan (the
+ * staged band wider than 256 columns, or an image edge not a multiple of 4).
+ * Solvers, projection sets and servers made before the call keep the variant
+ * they were made with (the plan keeps its earlier tables until it is
+ * destroyed).  Not thread-safe against concurrent calls on the same plan.
+ * The forward projector of the reference
+ * (helical/rebin/src/tracing.cpp:22-147 applied per ray) has no such knob. */
+int at_plan_set_forward_variant(at_plan *plan, int32_t views, int32_t rays, int32_t rows);
 void at_plan_destroy(at_plan *plan);
 int at_plan_get_stats(const at_plan *plan, at_plan_stats *out);
 /* Traversal of one ray as the device plan stores it: pixel indices and FP32
@@ -288,6 +306,7 @@ typedef struct at_server_stats {
     double slices_per_s;      /* completed / (last completion - first admitted arrival) */
     double busy_s;            /* time spent in rounds                                   */
     size_t peak_state_bytes;
+    int64_t psnr_stops;       /* requests finished by their quality target before iter_alt */
 } at_server_stats;
 int at_server_create(const at_server_config *cfg, at_server **out);
 void at_server_destroy(at_server *s);
@@ -298,6 +317,20 @@ int at_server_submit(at_server *s, at_plan *plan, const float *h_sino, int32_t i
 /* Serves until every queued request is done (or max_seconds passed). */
 int at_server_run(at_server *s, double max_seconds);
 int at_server_result(at_server *s, int64_t id, float *h_f, float *h_v, double *latency_s, double *wait_s);
+/* at_server_submit with a quality stop (the "equal PSNR" criterion of the
+ * serving benchmark): after every outer iteration the server measures
+ * PSNR(f, h_ref) on the GPU, 10 log10(peak^2 / MSE) as msbeam/CPU_OpenMP's
+ * PSNR.m:11 (peak <= 0: max of h_ref), and finishes the request as soon as it
+ * reaches target_psnr_db, or after iter_alt outer iterations.  h_ref (n x n,
+ * or nz x n x n) is copied and held in HBM with the request; it counts against
+ * the admission budget.  A request's result depends only on its data, so it
+ * stops at the same iteration alone and in any mix. */
+int at_server_submit_psnr(at_server *s, at_plan *plan, const float *h_sino, int32_t iter_alt, double arrival_s,
+                          const float *h_ref, double target_psnr_db, double peak, int64_t *id);
+/* Outer iterations a finished request ran, its last measured PSNR (NaN without
+ * a quality stop) and whether the quality target ended it before iter_alt. */
+int at_server_result_info(const at_server *s, int64_t id, int32_t *iterations, double *psnr_db,
+                          int32_t *stopped_by_psnr);
 int at_server_get_stats(const at_server *s, at_server_stats *out);
 
 /* ---- forward projection that allocates no device memory ----

@@ -18,7 +18,9 @@
 #include <cstddef>
 #include <cstdint>
 #include <string>
+#include <vector>
 
+#include <cuda.h>  // CUtensorMap (the descriptor type only; no driver calls are linked)
 #include <cuda_runtime.h>
 
 #include "../../include/at_engine.h"
@@ -51,6 +53,31 @@ struct GcEntry { // transposed entry at a symmetry-0 pixel
   float w;
 };
 
+// Forward projection through shared-memory slabs (slab.cu).  A CTA owns
+// `views` consecutive views x `rays` adjacent detectors; its rays run closer to
+// one image axis, and it reads the image copy (row-major, or transposed) in
+// which that axis is the row index.  The rows are cut into slabs of `rows`
+// rows; the CTA stages each slab's band of columns in shared memory by TMA
+// (double-buffered) and every thread walks its ray through the slab from
+// there, pausing at the slab's far edge.
+struct SlabPlan {
+  int ok = 0;      // tables built: the fan / ray-table forward projector uses slabs
+  int views = 0;   // views per CTA
+  int rays = 0;    // adjacent detectors per view per CTA (a divisor of 128)
+  int rows = 0;    // image rows per slab
+  int wbox = 0;    // staged columns per slab: the TMA box width, a multiple of 4
+  int nslab = 0;   // slabs of one copy: ceil(n / rows)
+  int ndb = 0;     // CTAs per view group: ceil(ndets / rays)
+  int ncta = 0;    // CTAs of one projection
+  int fallback = 0;  // CTAs that gather through L1 instead (rays off the grid)
+  uint4 *cta_d = nullptr;     // per CTA: x = first slab | last slab << 16 (in walk order), y = kSlab* flags
+  int16_t *wlo_d = nullptr;   // [ncta][nslab]: first staged column of each slab (a multiple of 4)
+};
+constexpr unsigned kSlabTransposed = 1u;  // the CTA reads the transposed copy
+constexpr unsigned kSlabDown = 2u;        // its rays run towards decreasing rows
+constexpr unsigned kSlabFallback = 4u;    // a ray leaves the grid or runs against the others: gather through L1
+constexpr unsigned kSlabEmpty = 8u;       // no ray of the CTA crosses the image
+
 struct Plan {
   int kind = AT_GEOM_FAN;
   at_fan_geometry geom{};
@@ -64,6 +91,10 @@ struct Plan {
   int max_segments = 0;
   int fp_rpt = 1;  // rays per thread of the forward projector (autotuned)
   int alpha_fp32 = 0;  // fan / ray plans traced in FP32 (the plain form) instead of FP64
+  SlabPlan slab;       // fan / ray plans: the slab forward projector's tables
+  // tables replaced by at_plan_set_forward_variant, kept until the plan is
+  // destroyed: batches built earlier still point at them
+  std::vector<SlabPlan> retired_slabs;
   // fan
   RayHdr *rays_d = nullptr;
   uint32_t *bits_d = nullptr;
@@ -125,6 +156,12 @@ int build_fan_plan(Plan &p, cudaStream_t st, const double *h_ends = nullptr);  /
 int validate_rays(int n, double pixel_mm, int nviews, int ndets, const double *h_ends);
 int build_goldnc_plan(Plan &p, cudaStream_t st);
 int autotune_fan(Plan &p, cudaStream_t st);
+// slab forward projector (slab.cu): tables for one CTA shape; 0 and p.slab.ok
+// = 0 when the shape does not fit (staged band wider than a TMA box, or the
+// grid's rows not 16-byte multiples)
+int build_slab_tables(Plan &p, int views, int rays, int rows, cudaStream_t st);
+void free_slab_tables(SlabPlan &s);
+void retire_slab_tables(Plan &p);  // moves p.slab to p.retired_slabs
 
 }  // namespace medimg
 

@@ -14,7 +14,8 @@
 namespace medimg {
 
 int fp_ctas(const ScanDev &S, int rpt);
-cudaError_t launch_fp_single_tr(const Launch &L, int rpt, int nctas, float *tr, cudaStream_t st);
+cudaError_t launch_fp_single(const Launch &L, const Plan &p, int rpt, void *scratch, cudaStream_t st);
+size_t fp_single_scratch_bytes(const Plan &p);
 int bp_ctas(const ScanDev &S);
 cudaError_t launch_fp(const Launch &L, int kind, int rpt, int nctas, cudaStream_t st);
 cudaError_t launch_bp(const Launch &L, int kind, int nctas, cudaStream_t st, const Launch *Lpix, int pix_nctas);
@@ -63,10 +64,10 @@ int project(const Plan &p, bool forward, const float *in, float *out, cudaStream
   if (forward) {
     const int rpt = projector_rpt(p);
     if (p.kind == AT_GEOM_FAN || p.kind == AT_GEOM_RAYS) {
-      // stream-ordered scratch for the image's transposed copy
-      float *tr = nullptr;
-      AT_CUDA_TRY(cudaMallocAsync(&tr, sizeof(float) * (size_t)p.n * p.n, st));
-      e = launch_fp_single_tr(L, rpt, fp_ctas(L.single, rpt), tr, st);
+      // stream-ordered scratch for the image's row-major and transposed copies
+      void *tr = nullptr;
+      AT_CUDA_TRY(cudaMallocAsync(&tr, fp_single_scratch_bytes(p), st));
+      e = launch_fp_single(L, p, rpt, tr, st);
       cudaFreeAsync(tr, st);
     } else {
       e = launch_fp(L, p.kind, rpt, fp_ctas(L.single, rpt), st);
@@ -221,6 +222,25 @@ AT_API int at_plan_create_goldnc(at_plan **out) {
 
 AT_API void at_plan_destroy(at_plan *plan) { delete plan; }
 
+AT_API int at_plan_set_forward_variant(at_plan *plan, int32_t views, int32_t rays, int32_t rows) {
+  AT_CHECK_ARG(plan, "at_plan_set_forward_variant: null plan");
+  Plan &p = plan->p;
+  AT_CHECK_ARG(p.kind == AT_GEOM_FAN || p.kind == AT_GEOM_RAYS,
+               "at_plan_set_forward_variant: fan-beam and ray-table plans only");
+  // the current tables may be bound into solvers or projection sets made
+  // earlier: retire them (freed with the plan) rather than free them
+  retire_slab_tables(p);
+  if (views == 0 && rays == 0 && rows == 0) return AT_OK;
+  cudaStream_t st;
+  AT_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  const int rc = build_slab_tables(p, views, rays, rows, st);
+  cudaStreamSynchronize(st);
+  cudaStreamDestroy(st);
+  if (rc) return rc;
+  if (!p.slab.ok) return set_error(AT_EINVAL, "at_plan_set_forward_variant: this slab shape does not fit the plan");
+  return AT_OK;
+}
+
 AT_API int at_plan_get_stats(const at_plan *plan, at_plan_stats *out) {
   AT_CHECK_ARG(plan && out, "at_plan_get_stats: null argument");
   const Plan &p = plan->p;
@@ -236,6 +256,11 @@ AT_API int at_plan_get_stats(const at_plan *plan, at_plan_stats *out) {
   out->fp_rays_per_thread = p.fp_rpt;
   out->bp_runs = p.nruns;
   out->nz = p.nz;
+  out->slab_views = p.slab.ok ? p.slab.views : 0;
+  out->slab_rays = p.slab.ok ? p.slab.rays : 0;
+  out->slab_rows = p.slab.ok ? p.slab.rows : 0;
+  out->slab_wbox = p.slab.ok ? p.slab.wbox : 0;
+  out->slab_fallback_ctas = p.slab.ok ? p.slab.fallback : 0;
   return AT_OK;
 }
 

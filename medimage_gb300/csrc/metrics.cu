@@ -91,6 +91,38 @@ __global__ void ssim_partial_kernel(const float *x, const float *y, int h, int w
 constexpr int kBlocks = 512, kThreads = 256;
 
 }  // namespace
+
+// device scratch of one PSNR evaluation (partial sums and maxima)
+size_t psnr_scratch_bytes() { return kBlocks * (sizeof(double) + sizeof(unsigned)); }
+
+// PSNR of d_x against d_ref (n values) on `st` with caller-owned scratch of
+// psnr_scratch_bytes(); peak <= 0 takes max(ref).  Waits for the stream.
+int psnr_with_scratch(const float *d_x, const float *d_ref, int64_t n, double peak, void *scratch, double *h_psnr,
+                      cudaStream_t st) {
+  double *psum = reinterpret_cast<double *>(scratch);
+  unsigned *pmax = reinterpret_cast<unsigned *>(psum + kBlocks);
+  psnr_partial_kernel<<<kBlocks, kThreads, 0, st>>>(d_x, d_ref, n, psum, pmax);
+  AT_CUDA_TRY(cudaGetLastError());
+  double hs[kBlocks];
+  unsigned hm[kBlocks];
+  AT_CUDA_TRY(cudaMemcpyAsync(hs, psum, sizeof(hs), cudaMemcpyDeviceToHost, st));
+  AT_CUDA_TRY(cudaMemcpyAsync(hm, pmax, sizeof(hm), cudaMemcpyDeviceToHost, st));
+  AT_CUDA_TRY(cudaStreamSynchronize(st));
+  double sum = 0.0;
+  unsigned m = 0u;
+  for (int b = 0; b < kBlocks; b++) {
+    sum += hs[b];
+    m = hm[b] > m ? hm[b] : m;
+  }
+  const unsigned u = (m & 0x80000000u) ? (m & 0x7fffffffu) : ~m;
+  float maxref;
+  std::memcpy(&maxref, &u, sizeof(float));
+  const double pk = peak > 0 ? peak : (double)maxref;
+  const double mse = sum / (double)n;
+  *h_psnr = mse == 0.0 ? INFINITY : 10.0 * std::log10(pk * pk / mse);
+  return AT_OK;
+}
+
 }  // namespace medimg
 
 using namespace medimg;
@@ -100,34 +132,12 @@ using namespace medimg;
 AT_API int at_psnr(const float *d_x, const float *d_ref, int64_t n, double peak, double *h_psnr, void *stream) {
   if (!d_x || !d_ref || !h_psnr || n <= 0) return set_error(AT_EINVAL, "at_psnr: bad argument");
   cudaStream_t st = (cudaStream_t)stream;
-  double *psum = nullptr;
-  unsigned *pmax = nullptr;
+  void *scratch = nullptr;
   const auto free_temps = scope_exit([&] {
-    if (psum) cudaFreeAsync(psum, st);
-    if (pmax) cudaFreeAsync(pmax, st);
+    if (scratch) cudaFreeAsync(scratch, st);
   });
-  AT_CUDA_TRY(cudaMallocAsync(&psum, sizeof(double) * kBlocks, st));
-  AT_CUDA_TRY(cudaMallocAsync(&pmax, sizeof(unsigned) * kBlocks, st));
-  psnr_partial_kernel<<<kBlocks, kThreads, 0, st>>>(d_x, d_ref, n, psum, pmax);
-  AT_CUDA_TRY(cudaGetLastError());
-  double hs[kBlocks];
-  unsigned hm[kBlocks];
-  AT_CUDA_TRY(cudaMemcpyAsync(hs, psum, sizeof(hs), cudaMemcpyDeviceToHost, st));
-  AT_CUDA_TRY(cudaMemcpyAsync(hm, pmax, sizeof(hm), cudaMemcpyDeviceToHost, st));
-  AT_CUDA_TRY(cudaStreamSynchronize(st));
-  double s = 0.0;
-  unsigned m = 0u;
-  for (int b = 0; b < kBlocks; b++) {
-    s += hs[b];
-    m = hm[b] > m ? hm[b] : m;
-  }
-  const unsigned u = (m & 0x80000000u) ? (m & 0x7fffffffu) : ~m;
-  float maxref;
-  std::memcpy(&maxref, &u, sizeof(float));
-  const double pk = peak > 0 ? peak : (double)maxref;
-  const double mse = s / (double)n;
-  *h_psnr = mse == 0.0 ? INFINITY : 10.0 * std::log10(pk * pk / mse);
-  return AT_OK;
+  AT_CUDA_TRY(cudaMallocAsync(&scratch, psnr_scratch_bytes(), st));
+  return psnr_with_scratch(d_x, d_ref, n, peak, scratch, h_psnr, st);
 }
 
 AT_API int at_ssim(const float *d_x, const float *d_ref, int32_t h, int32_t w, double dynamic_range, double *h_ssim,

@@ -730,6 +730,8 @@ Plan::~Plan() {
   cudaFree(gc_ent_d);
   cudaFree(gc_pix_off_d);
   cudaFree(cone_trig_d);
+  free_slab_tables(slab);
+  for (auto &r : retired_slabs) free_slab_tables(r);
 }
 
 }  // namespace medimg

@@ -68,10 +68,13 @@ __global__ void __launch_bounds__(256) fp_pack_kernel(const Launch L, int bins) 
   const int cta0 = __ldg(L.prefix + scan), ncta = __ldg(L.prefix + scan + 1) - cta0;
   const int n = S.n, npix = n * n;
   const int count = bins ? S.nbins : npix;
-  if (S.nmem == 1) {  // a scan alone: only the transposed image, as floats
+  if (S.nmem == 1) {  // a scan alone: the image as floats, row-major then transposed
     float *t = reinterpret_cast<float *>(S.pack);
-    for (int p = (blockIdx.x - cta0) * blockDim.x + threadIdx.x; p < npix; p += ncta * blockDim.x)
-      t[(p % n) * n + p / n] = src[0] ? __ldg(src[0] + p) : 0.f;
+    for (int p = (blockIdx.x - cta0) * blockDim.x + threadIdx.x; p < npix; p += ncta * blockDim.x) {
+      const float v = src[0] ? __ldg(src[0] + p) : 0.f;
+      t[p] = v;
+      t[npix + (p % n) * n + p / n] = v;
+    }
     return;
   }
   for (int p = (blockIdx.x - cta0) * blockDim.x + threadIdx.x; p < count; p += ncta * blockDim.x) {
@@ -168,7 +171,7 @@ __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
       if (!__ldg(S.blk_off + blk) && lx0 > ly0) {
         pk4 += npix;
         pk2 += npix;
-        if constexpr (G == 1) img = reinterpret_cast<const float *>(S.pack);
+        if constexpr (G == 1) img = reinterpret_cast<const float *>(S.pack) + npix;
 #pragma unroll
         for (int r = 0; r < RPT; r++) {
           if (nseg[r] == 0) continue;
@@ -734,6 +737,9 @@ __global__ void __launch_bounds__(256) gc_bp_kernel(const Launch L) {
 // ---------------------------------------------------------------------------
 int cone_ctas(const ScanDev &S);
 cudaError_t launch_cone_fp(const Launch &L, int nctas, cudaStream_t st);
+cudaError_t launch_fp_slab(const Launch &L, int G, int nctas, int threads, size_t smem, cudaStream_t st);
+size_t slab_smem_bytes(int G, int rows, int wbox);
+int encode_pack_tmap(CUtensorMap *out, const void *pack, int n, int G, int wbox, int rows);
 cudaError_t launch_cone_bp(const Launch &L, int nctas, const Launch &Lpix, int pix_nctas, cudaStream_t st);
 
 int fp_ctas(const ScanDev &S, int rpt) {
@@ -788,9 +794,21 @@ cudaError_t launch_fp(const Launch &L, int kind, int rpt, int nctas, cudaStream_
 // form: groups of three or four over L's CTAs, scans alone over L1's, pairs
 // over L2's.  Returns the number of launches.
 int launch_fp_group(const Launch &L, const Launch &Lpix, const Launch &L1, const Launch &L2, int nctas, int pix_nctas,
-                    int nctas1, int nctas2, cudaStream_t st) {
+                    int nctas1, int nctas2, const SlabLaunch *slab, cudaStream_t st) {
   int n = 1;
   fp_pack_kernel<<<pix_nctas, 256, 0, st>>>(Lpix, 0);
+  if (slab) {  // every plan of the batch has slab tables of one CTA shape
+    const int G[3] = {kGroupMax, 1, 2};
+    const Launch *Ls[3] = {&L, &L1, &L2};
+    const int nc[3] = {nctas, nctas1, nctas2};
+    for (int i = 0; i < 3; i++) {
+      if (nc[i] <= 0) continue;
+      const cudaError_t e = launch_fp_slab(*Ls[i], G[i], nc[i], slab->threads, slab->smem[i], st);
+      if (e != cudaSuccess) return -1;
+      n++;
+    }
+    return n;
+  }
   Launch Lg = L, Lg1 = L1, Lg2 = L2;
   Lg.tr = Lg1.tr = Lg2.tr = 1;
   if (nctas > 0) {
@@ -808,41 +826,75 @@ int launch_fp_group(const Launch &L, const Launch &Lpix, const Launch &L1, const
   return n;
 }
 
-// out[y][x] = in[x][y] for an n x n image, through 32 x 32 shared-memory tiles
-// (coalesced reads and writes)
-__global__ void __launch_bounds__(256) transpose_kernel(const float *__restrict__ in, float *__restrict__ out,
-                                                         int n) {
+// out[p] = in[p] and out[n*n + y*n + x] = in[x*n + y] for an n x n image
+// (the row-major and transposed copies the forward projectors read), through
+// 32 x 32 shared-memory tiles (coalesced reads and writes)
+__global__ void __launch_bounds__(256) pack_single_kernel(const float *__restrict__ in, float *__restrict__ out,
+                                                           int n) {
   __shared__ float t[32][33];
   const int bx = blockIdx.x * 32, by = blockIdx.y * 32;
+  const size_t npix = (size_t)n * n;
   for (int r = threadIdx.y; r < 32; r += 8) {
     const int x = by + r, y = bx + threadIdx.x;
-    if (x < n && y < n) t[r][threadIdx.x] = in[(size_t)x * n + y];
+    if (x < n && y < n) {
+      const float v = in[(size_t)x * n + y];
+      t[r][threadIdx.x] = v;
+      out[(size_t)x * n + y] = v;
+    }
   }
   __syncthreads();
   for (int r = threadIdx.y; r < 32; r += 8) {
     const int y = bx + r, x = by + threadIdx.x;
-    if (x < n && y < n) out[(size_t)y * n + x] = t[threadIdx.x][r];
+    if (x < n && y < n) out[npix + (size_t)y * n + x] = t[threadIdx.x][r];
   }
 }
 
-// One fan-beam / ray-table forward projection outside a batch, reading its
-// image's transposed copy (`tr`, n x n floats of scratch) where the rays run
-// closer to the y axis.
-cudaError_t launch_fp_single_tr(const Launch &L, int rpt, int nctas, float *tr, cudaStream_t st) {
+// Device scratch of one fan-beam / ray-table forward projection outside a
+// batch: the image's two copies (2 n^2 floats) and, for the slab projector,
+// its TMA descriptor.
+size_t fp_single_scratch_bytes(const Plan &p) {
+  return ((sizeof(float) * 2 * (size_t)p.n * p.n + 255) & ~(size_t)255) + sizeof(CUtensorMap);
+}
+
+// One fan-beam / ray-table forward projection outside a batch: the image's
+// row-major and transposed copies into `scratch` (fp_single_scratch_bytes),
+// then the slab projector when the plan has slab tables, else the L1 walk
+// reading the transposed copy where rays run closer to the y axis.  The TMA
+// descriptor is copied from host memory that lives only through this call:
+// pageable cudaMemcpyAsync stages it before returning.
+cudaError_t launch_fp_single(const Launch &L, const Plan &p, int rpt, void *scratch, cudaStream_t st) {
   const int n = L.single.n;
-  transpose_kernel<<<dim3((n + 31) / 32, (n + 31) / 32), dim3(32, 8), 0, st>>>(L.single.buf[L.in_buf], tr, n);
+  float *copies = reinterpret_cast<float *>(scratch);
+  pack_single_kernel<<<dim3((n + 31) / 32, (n + 31) / 32), dim3(32, 8), 0, st>>>(L.single.buf[L.in_buf], copies, n);
   Launch Lt = L;
-  Lt.single.pack = reinterpret_cast<float4 *>(tr);
+  Lt.single.pack = reinterpret_cast<float4 *>(copies);
+  if (p.slab.ok) {
+    CUtensorMap *dmap = reinterpret_cast<CUtensorMap *>(reinterpret_cast<char *>(scratch) +
+                                                        fp_single_scratch_bytes(p) - sizeof(CUtensorMap));
+    CUtensorMap hmap;
+    if (encode_pack_tmap(&hmap, copies, n, 1, p.slab.wbox, p.slab.rows)) return cudaErrorInvalidValue;
+    cudaError_t e = cudaMemcpyAsync(dmap, &hmap, sizeof(hmap), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return e;
+    Lt.single.tmap = dmap;
+    return launch_fp_slab(Lt, 1, p.slab.ncta, p.slab.views * p.slab.rays,
+                          slab_smem_bytes(1, p.slab.rows, p.slab.wbox), st);
+  }
   Lt.tr = 1;
-  return launch_fp(Lt, AT_GEOM_FAN, rpt, nctas, st);
+  return launch_fp(Lt, AT_GEOM_FAN, rpt, fp_ctas(L.single, rpt), st);
 }
 
 // Forward projection of a batch of fan-beam / ray-table scans without groups:
-// each scan's input transposed into its pack buffer (over the pixel-pass CTAs
-// of Lpix), then the walk with RPT rays per thread.  Returns the number of
-// launches.
-int launch_fp_tr(const Launch &L, const Launch &Lpix, int rpt, int nctas, int pix_nctas, cudaStream_t st) {
+// each scan's input copied row-major and transposed into its pack buffer (over
+// the pixel-pass CTAs of Lpix), then the slab projector (`slab`: every plan has
+// slab tables of one CTA shape) or the L1 walk with RPT rays per thread.
+// Returns the number of launches.
+int launch_fp_tr(const Launch &L, const Launch &Lpix, int rpt, int nctas, int pix_nctas, const SlabLaunch *slab,
+                 cudaStream_t st) {
   fp_pack_kernel<<<pix_nctas, 256, 0, st>>>(Lpix, 0);
+  if (slab) {
+    if (launch_fp_slab(L, 1, nctas, slab->threads, slab->smem[1], st) != cudaSuccess) return -1;
+    return 2;
+  }
   Launch Lt = L;
   Lt.tr = 1;
   launch_fp(Lt, AT_GEOM_FAN, rpt, nctas, st);
@@ -890,26 +942,35 @@ cudaError_t launch_bp(const Launch &L, int kind, int nctas, cudaStream_t st, con
 
 namespace medimg {
 
-// Times the forward projector with 1, 2 and 4 rays per thread on this plan and
-// keeps the fastest (results are bitwise identical across the three).
+size_t fp_single_scratch_bytes(const Plan &p);
+cudaError_t launch_fp_single(const Launch &L, const Plan &p, int rpt, void *scratch, cudaStream_t st);
+
+// Times the plan's forward projector variants on a zero image and keeps the
+// fastest (results are bitwise identical across all of them): the L1 walk
+// with 1, 2 and 4 rays per thread, and the slab projector for a few CTA
+// shapes (views x rays per CTA, rows per slab).  Each variant is timed as a
+// projection outside a batch, the image's copies included.
 int autotune_fan(Plan &p, cudaStream_t st) {
   p.fp_rpt = 1;
+  free_slab_tables(p.slab);
   if (p.kind == AT_GEOM_GOLDNC || p.kind == AT_GEOM_CONE) return AT_OK;
   float *img = nullptr, *sino = nullptr;
+  void *scratch = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   const auto free_temps = scope_exit([&] {
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
     if (img) cudaFreeAsync(img, st);
     if (sino) cudaFreeAsync(sino, st);
+    if (scratch) cudaFreeAsync(scratch, st);
   });
   const size_t npix = (size_t)p.n * p.n, nbins = (size_t)p.nviews * p.ndets;
   AT_CUDA_TRY(cudaMallocAsync(&img, npix * sizeof(float), st));
   AT_CUDA_TRY(cudaMallocAsync(&sino, nbins * sizeof(float), st));
+  AT_CUDA_TRY(cudaMallocAsync(&scratch, fp_single_scratch_bytes(p), st));
   AT_CUDA_TRY(cudaMemsetAsync(img, 0, npix * sizeof(float), st));
   Launch L;
   memset(&L, 0, sizeof(L));
-  fill_scan_plan(L.single, p);
   L.single.buf[0] = img;
   L.single.buf[1] = sino;
   L.nscans = 1;
@@ -920,20 +981,45 @@ int autotune_fan(Plan &p, cudaStream_t st) {
   L.aux_buf = -1;
   AT_CUDA_TRY(cudaEventCreate(&e0));
   AT_CUDA_TRY(cudaEventCreate(&e1));
-  float best = 1e30f;
-  const int cands[3] = {1, 2, 4};
-  for (int rpt : cands) {
-    AT_CUDA_TRY(launch_fp(L, p.kind, rpt, fp_ctas(L.single, rpt), st));
+  auto time_it = [&](int rpt, float &ms) -> int {
+    fill_scan_plan(L.single, p);
+    L.single.buf[0] = img;
+    L.single.buf[1] = sino;
+    AT_CUDA_TRY(launch_fp_single(L, p, rpt, scratch, st));
     AT_CUDA_TRY(cudaEventRecord(e0, st));
-    for (int i = 0; i < 3; i++) AT_CUDA_TRY(launch_fp(L, p.kind, rpt, fp_ctas(L.single, rpt), st));
+    for (int i = 0; i < 3; i++) AT_CUDA_TRY(launch_fp_single(L, p, rpt, scratch, st));
     AT_CUDA_TRY(cudaEventRecord(e1, st));
     AT_CUDA_TRY(cudaEventSynchronize(e1));
-    float ms = 0.f;
     AT_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+    return AT_OK;
+  };
+  float best = 1e30f;
+  int rc;
+  for (int rpt : {1, 2, 4}) {
+    float ms = 0.f;
+    if ((rc = time_it(rpt, ms))) return rc;
     if (ms < best) {
       best = ms;
       p.fp_rpt = rpt;
     }
+  }
+  // slab shapes: views x rays per CTA (at most 512 threads), rows per slab
+  const int shapes[][3] = {{4, 128, 16}, {2, 128, 16}, {4, 128, 8}, {8, 64, 16}, {4, 64, 16}, {2, 128, 32}};
+  int pick = -1;
+  for (int i = 0; i < (int)(sizeof(shapes) / sizeof(shapes[0])); i++) {
+    if ((rc = build_slab_tables(p, shapes[i][0], shapes[i][1], shapes[i][2], st))) return rc;
+    if (!p.slab.ok) continue;
+    float ms = 0.f;
+    if ((rc = time_it(p.fp_rpt, ms))) return rc;
+    if (ms < best) {
+      best = ms;
+      pick = i;
+    }
+  }
+  if (pick >= 0) {
+    if ((rc = build_slab_tables(p, shapes[pick][0], shapes[pick][1], shapes[pick][2], st))) return rc;
+  } else {
+    free_slab_tables(p.slab);
   }
   AT_CUDA_TRY(cudaStreamSynchronize(st));
   return AT_OK;

@@ -17,6 +17,7 @@
 // same alone and in any mix.
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -28,6 +29,9 @@
 namespace medimg {
 
 cudaError_t launch_fill(float *p, float v, size_t n, cudaStream_t st);
+size_t psnr_scratch_bytes();
+int psnr_with_scratch(const float *d_x, const float *d_ref, int64_t n, double peak, void *scratch, double *h_psnr,
+                      cudaStream_t st);
 
 namespace {
 double now_s() {
@@ -59,6 +63,12 @@ struct Request {
   double t_admit = 0.0, t_done = 0.0;
   Ctl ctl{};
   std::vector<float> f, v;
+  // quality stop: the request finishes as soon as PSNR(f, ref) >= target
+  // (measured on the GPU after every outer iteration), or after iter_alt
+  std::vector<float> ref;
+  float *d_ref = nullptr;  // in the request's state allocation
+  double target_psnr = 0.0, peak = 0.0, psnr = NAN;
+  bool psnr_stop = false;
 };
 
 // The requests of one geometry: one batch, advanced one outer iteration per
@@ -70,11 +80,13 @@ struct Group {
   Batch batch;
   cudaStream_t st = nullptr;
   cudaEvent_t ev = nullptr;
+  void *psnr_scratch = nullptr;  // partial sums of the quality checks
   std::vector<Request *> active;
   std::vector<Request *> round;  // the requests the round in flight advances
   bool dirty = true, in_flight = false;
   double r0 = 0.0;
   ~Group() {
+    if (psnr_scratch) cudaFree(psnr_scratch);
     if (ev) cudaEventDestroy(ev);
     if (st) cudaStreamDestroy(st);
   }
@@ -91,7 +103,7 @@ struct Server {
   int nactive = 0;
   int64_t next_id = 1;
   size_t used = 0, peak = 0;
-  int64_t rounds = 0, completed = 0;
+  int64_t rounds = 0, completed = 0, psnr_stops = 0;
   double t0 = -1.0, busy = 0.0, t_first = -1.0, t_last = 0.0;
   int64_t slices = 0;
 
@@ -111,9 +123,16 @@ struct Server {
       g->batch.params = prm;
       AT_CUDA_TRY(cudaStreamCreateWithFlags(&g->st, cudaStreamNonBlocking));
       AT_CUDA_TRY(cudaEventCreateWithFlags(&g->ev, cudaEventDisableTiming));
+      AT_CUDA_TRY(cudaMalloc(&g->psnr_scratch, psnr_scratch_bytes()));
     }
     *out = g.get();
     return AT_OK;
+  }
+
+  // device bytes of a request: its solver state, and its reference image
+  // when it has a quality stop
+  size_t request_bytes(const Request &r) const {
+    return scan_bytes(*r.plan, rpt) + ((sizeof(float) * r.ref.size() + 255) & ~(size_t)255);
   }
 
   int admit(Request *r, double t) {
@@ -121,10 +140,14 @@ struct Server {
     int rc = group_of(r->plan, &g);
     if (rc) return rc;
     cudaStream_t gs = g->st;
-    r->bytes = scan_bytes(*r->plan, rpt);
+    r->bytes = request_bytes(*r);
     cudaError_t e = cudaMallocAsync(&r->mem, r->bytes, gs);
     if (e != cudaSuccess) return cuda_error(e, "server: state allocation");
     carve_scan(r->dev, *r->plan, rpt, (char *)r->mem);
+    if (!r->ref.empty()) {
+      r->d_ref = reinterpret_cast<float *>((char *)r->mem + scan_bytes(*r->plan, rpt));
+      AT_CUDA_TRY(cudaMemcpyAsync(r->d_ref, r->ref.data(), sizeof(float) * r->ref.size(), cudaMemcpyHostToDevice, gs));
+    }
     r->ctl = make_ctl(prm);
     AT_CUDA_TRY(cudaMemcpyAsync(r->dev.ctl, &r->ctl, sizeof(Ctl), cudaMemcpyHostToDevice, gs));
     AT_CUDA_TRY(cudaMemcpyAsync(r->dev.buf[B_G], r->sino.data(), sizeof(float) * r->sino.size(),
@@ -155,8 +178,11 @@ struct Server {
     used -= r->bytes;
     r->state = 2;
     r->t_done = t;
+    r->d_ref = nullptr;
     r->sino.clear();
     r->sino.shrink_to_fit();
+    r->ref.clear();
+    r->ref.shrink_to_fit();
     completed++;
     slices++;
     nactive--;
@@ -175,7 +201,7 @@ struct Server {
       // admission: arrived requests in order, while slots and budget allow
       while (!pending.empty() && pending.front()->arrival <= t && nactive < cfg.max_active) {
         Request *r = pending.front();
-        if (used + scan_bytes(*r->plan, rpt) > cfg.hbm_budget_bytes) {
+        if (used + request_bytes(*r) > cfg.hbm_budget_bytes) {
           if (nactive == 0) return set_error(AT_EBUDGET, "server: request does not fit the HBM budget");
           break;
         }
@@ -221,8 +247,20 @@ struct Server {
         g->in_flight = false;
         progressed = true;
         for (auto *r : g->round) {
-          if (++r->iters_done >= r->iter_alt) {
-            if ((rc = retire(g, r, r1 - t0))) return rc;
+          ++r->iters_done;
+          bool done = r->iters_done >= r->iter_alt;
+          if (r->target_psnr > 0) {  // the quality stop, on the GPU
+            if ((rc = psnr_with_scratch(r->dev.buf[B_F], r->d_ref, r->dev.npix, r->peak, g->psnr_scratch, &r->psnr,
+                                        g->st)))
+              return rc;
+            if (r->psnr >= r->target_psnr) {
+              r->psnr_stop = !done;
+              psnr_stops += r->psnr_stop ? 1 : 0;
+              done = true;
+            }
+          }
+          if (done) {
+            if ((rc = retire(g, r, now_s() - t0))) return rc;
             g->active.erase(std::find(g->active.begin(), g->active.end(), r));
           }
         }
@@ -288,6 +326,38 @@ AT_API int at_server_submit(at_server *srv, at_plan *plan, const float *h_sino, 
   return AT_OK;
 }
 
+AT_API int at_server_submit_psnr(at_server *srv, at_plan *plan, const float *h_sino, int32_t iter_alt,
+                                 double arrival_s, const float *h_ref, double target_psnr_db, double peak,
+                                 int64_t *id) {
+  if (!srv || !h_ref || !(target_psnr_db > 0))
+    return set_error(AT_EINVAL, "at_server_submit_psnr: a reference image and a positive target are required");
+  if (!plan || !id) return set_error(AT_EINVAL, "at_server_submit_psnr: null argument");
+  Server &S = srv->s;
+  const size_t npix = (size_t)plan->p.nz * plan->p.n * plan->p.n;
+  if (scan_bytes(plan->p, S.rpt) + sizeof(float) * npix + 256 > S.cfg.hbm_budget_bytes)
+    return set_error(AT_EBUDGET, "at_server_submit_psnr: the request alone exceeds the HBM admission budget");
+  const int rc = at_server_submit(srv, plan, h_sino, iter_alt, arrival_s, id);
+  if (rc) return rc;
+  Request &r = *S.reqs[*id];
+  r.ref.assign(h_ref, h_ref + npix);
+  r.target_psnr = target_psnr_db;
+  r.peak = peak;
+  return AT_OK;
+}
+
+AT_API int at_server_result_info(const at_server *srv, int64_t id, int32_t *iterations, double *psnr_db,
+                                 int32_t *stopped_by_psnr) {
+  if (!srv) return set_error(AT_EINVAL, "at_server_result_info: null argument");
+  auto it = srv->s.reqs.find(id);
+  if (it == srv->s.reqs.end()) return set_error(AT_EINVAL, "at_server_result_info: unknown request");
+  const Request &r = *it->second;
+  if (r.state != 2) return set_error(AT_ESTATE, "at_server_result_info: request not finished");
+  if (iterations) *iterations = r.iters_done;
+  if (psnr_db) *psnr_db = r.psnr;
+  if (stopped_by_psnr) *stopped_by_psnr = r.psnr_stop ? 1 : 0;
+  return AT_OK;
+}
+
 AT_API int at_server_run(at_server *srv, double max_seconds) {
   if (!srv) return set_error(AT_EINVAL, "at_server_run: null argument");
   return srv->s.run(max_seconds > 0 ? max_seconds : 1e30);
@@ -323,5 +393,6 @@ AT_API int at_server_get_stats(const at_server *srv, at_server_stats *out) {
   out->slices_per_s = span > 0 ? S.completed / span : 0.0;
   out->busy_s = S.busy;
   out->peak_state_bytes = S.peak;
+  out->psnr_stops = S.psnr_stops;
   return AT_OK;
 }

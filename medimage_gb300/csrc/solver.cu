@@ -22,8 +22,12 @@ int bp_ctas(const ScanDev &S);
 int pix_ctas(const ScanDev &S);
 cudaError_t launch_fp(const Launch &L, int kind, int rpt, int nctas, cudaStream_t st);
 int launch_fp_group(const Launch &L, const Launch &Lpix, const Launch &L1, const Launch &L2, int nctas, int pix_nctas,
-                    int nctas1, int nctas2, cudaStream_t st);
-int launch_fp_tr(const Launch &L, const Launch &Lpix, int rpt, int nctas, int pix_nctas, cudaStream_t st);
+                    int nctas1, int nctas2, const SlabLaunch *slab, cudaStream_t st);
+int launch_fp_tr(const Launch &L, const Launch &Lpix, int rpt, int nctas, int pix_nctas, const SlabLaunch *slab,
+                 cudaStream_t st);
+int slab_ctas(const ScanDev &S);
+size_t slab_smem_bytes(int G, int rows, int wbox);
+int encode_pack_tmap(CUtensorMap *out, const void *pack, int n, int G, int wbox, int rows);
 int launch_bp_group(const Launch &L, const Launch &Lsino, const Launch &Lsmall, int nctas, int sino_nctas,
                     int small_nctas, cudaStream_t st);
 cudaError_t launch_bp(const Launch &L, int kind, int nctas, cudaStream_t st, const Launch *Lpix, int pix_nctas);
@@ -64,6 +68,16 @@ void fill_scan_plan(ScanDev &S, const Plan &p) {
   S.sod = p.cone.sod_mm;
   S.sdd = p.cone.sdd_mm;
   S.cone_trig = p.cone_trig_d;
+  if (p.slab.ok) {
+    S.slab_views = p.slab.views;
+    S.slab_rays = p.slab.rays;
+    S.slab_rows = p.slab.rows;
+    S.slab_wbox = p.slab.wbox;
+    S.slab_nslab = p.slab.nslab;
+    S.slab_ndb = p.slab.ndb;
+    S.slab_cta = p.slab.cta_d;
+    S.slab_wlo = p.slab.wlo_d;
+  }
 }
 
 namespace {
@@ -85,7 +99,7 @@ ScanLayout layout_of(const Plan &p, int rpt) {
   tmp.bp_split = kBpMaxSplit;  // size the partials for the largest split
   // and for one ray per thread (what grouped forward projections use)
   const int maxcta = std::max({fp_ctas(tmp, rpt), fp_group_ctas(tmp), bp_ctas(tmp), pix_ctas(tmp),
-                               (int)((nbins + 255) / 256)});
+                               (int)((nbins + 255) / 256), p.slab.ok ? p.slab.ncta : 0});
   L.partial_bytes = align_up((size_t)maxcta * 4 * sizeof(double));
   L.trace_bytes = align_up((size_t)kTraceCap * 10 * sizeof(double));
   L.bp_bytes = bp_scratch_bytes(p);
@@ -157,6 +171,7 @@ Ctl make_ctl(const at_params &prm) {
 Batch::~Batch() {
   cudaFree(scans_d);
   cudaFree(prefix_d);
+  cudaFree(tmaps_d);
 }
 
 int Batch::set(const ScanDev *scans, int n, int kind_, int rpt_, cudaStream_t st) {
@@ -166,11 +181,14 @@ int Batch::set(const ScanDev *scans, int n, int kind_, int rpt_, cudaStream_t st
   if (n > cap) {
     cudaFree(scans_d);
     cudaFree(prefix_d);
+    cudaFree(tmaps_d);
     scans_d = nullptr;
     prefix_d = nullptr;
+    tmaps_d = nullptr;
     cap = std::max(n, 2 * cap);
     AT_CUDA_TRY(cudaMalloc(&scans_d, sizeof(ScanDev) * cap));
     AT_CUDA_TRY(cudaMalloc(&prefix_d, sizeof(int) * kFamilies * (cap + 1)));
+    AT_CUDA_TRY(cudaMalloc(&tmaps_d, sizeof(CUtensorMap) * cap));
   }
   nscans = n;
   std::vector<ScanDev> sc(scans, scans + n);
@@ -202,6 +220,28 @@ int Batch::set(const ScanDev *scans, int n, int kind_, int rpt_, cudaStream_t st
     const int split = bp_split_for(tiles, nvb);
     for (auto &S : sc) S.bp_split = split;
   }
+  // the slab forward projector, when every plan has slab tables of one CTA
+  // shape: each lead's TMA descriptor covers its pack buffer in its group's
+  // form, and the launch's shared memory the largest slab buffers
+  slab = (kind == AT_GEOM_FAN || kind == AT_GEOM_RAYS);
+  for (const auto &S : sc)
+    slab = slab && S.slab_cta && S.pack && S.slab_views == sc[0].slab_views && S.slab_rays == sc[0].slab_rays;
+  std::vector<CUtensorMap> maps;
+  if (slab) {
+    slab_launch = SlabLaunch{sc[0].slab_views * sc[0].slab_rays, {0, 0, 0}};
+    maps.resize(n);
+    for (int s = 0; s < n; s++) {
+      ScanDev &S = sc[s];
+      const int G = S.nmem >= 3 ? 4 : S.nmem == 2 ? 2 : 1;
+      const int form = G == 4 ? 0 : G == 1 ? 1 : 2;
+      slab_launch.smem[form] = std::max(slab_launch.smem[form], slab_smem_bytes(G, S.slab_rows, S.slab_wbox));
+      S.tmap = tmaps_d + s;
+      if (S.nmem == 0) continue;  // a member: its lead's walk reads the group's pack buffer
+      int rc = encode_pack_tmap(&maps[s], S.pack, S.n, G, S.slab_wbox, S.slab_rows);
+      if (rc) return rc;
+    }
+    AT_CUDA_TRY(cudaMemcpyAsync(tmaps_d, maps.data(), sizeof(CUtensorMap) * n, cudaMemcpyHostToDevice, st));
+  }
   scans = sc.data();
   std::vector<int> pref(kFamilies * (n + 1), 0);
   auto add = [&](int fam, int s, int ctas) { pref[fam * (n + 1) + s + 1] = pref[fam * (n + 1) + s] + ctas; };
@@ -211,13 +251,14 @@ int Batch::set(const ScanDev *scans, int n, int kind_, int rpt_, cudaStream_t st
       // grouped projectors walk one ray per thread; groups of three or four
       // and the rest (pairs, scans alone) in launches of their own
       const bool big = nm >= 3, small = nm == 1 || nm == 2;
-      add(FAM_FP, s, big ? fp_group_ctas(scans[s]) : 0);
-      add(FAM_FP1, s, nm == 1 ? fp_group_ctas(scans[s]) : 0);
-      add(FAM_FP2, s, nm == 2 ? fp_group_ctas(scans[s]) : 0);
+      const int fpc = slab ? slab_ctas(scans[s]) : fp_group_ctas(scans[s]);
+      add(FAM_FP, s, big ? fpc : 0);
+      add(FAM_FP1, s, nm == 1 ? fpc : 0);
+      add(FAM_FP2, s, nm == 2 ? fpc : 0);
       add(FAM_BP, s, big ? bp_ctas(scans[s]) : 0);
       add(FAM_BPS, s, small ? bp_ctas(scans[s]) : 0);
     } else {
-      add(FAM_FP, s, fp_ctas(scans[s], rpt));
+      add(FAM_FP, s, slab ? slab_ctas(scans[s]) : fp_ctas(scans[s], rpt));
       add(FAM_FP1, s, 0);
       add(FAM_FP2, s, 0);
       add(FAM_BP, s, bp_ctas(scans[s]));
@@ -256,13 +297,18 @@ int Batch::enqueue_fp(const Launch &L, cudaStream_t st) {
     Lp.prefix = prefix_d + FAM_PIX * (nscans + 1);
     L1.prefix = prefix_d + FAM_FP1 * (nscans + 1);
     L2.prefix = prefix_d + FAM_FP2 * (nscans + 1);
-    launches += launch_fp_group(L, Lp, L1, L2, fp_total, pix_total, fp1_total, fp2_total, st);
+    const int nl = launch_fp_group(L, Lp, L1, L2, fp_total, pix_total, fp1_total, fp2_total,
+                                   slab ? &slab_launch : nullptr, st);
     AT_CUDA_TRY(cudaGetLastError());
+    if (nl < 0) return set_error(AT_ECUDA, "grouped forward projection launch failed");
+    launches += nl;
   } else if (kind == AT_GEOM_FAN || kind == AT_GEOM_RAYS) {  // transpose each input, then walk
     Launch Lp = L;
     Lp.prefix = prefix_d + FAM_PIX * (nscans + 1);
-    launches += launch_fp_tr(L, Lp, rpt, fp_total, pix_total, st);
+    const int nl = launch_fp_tr(L, Lp, rpt, fp_total, pix_total, slab ? &slab_launch : nullptr, st);
     AT_CUDA_TRY(cudaGetLastError());
+    if (nl < 0) return set_error(AT_ECUDA, "forward projection launch failed");
+    launches += nl;
   } else {
     AT_CUDA_TRY(launch_fp(L, kind, rpt, fp_total, st));
     launches++;

@@ -37,6 +37,12 @@ struct Batch {
   int *prefix_d = nullptr;  // [kFamilies][cap+1]: CTAs per scan of each family
   int fp_total = 0, pix_total = 0, sino_total = 0, bp_total = 0, fp1_total = 0, fp2_total = 0, bps_total = 0;
   int group = 1;            // largest group of scans sharing a plan (projected together)
+  // slab forward projector: used when every plan of the batch has slab tables
+  // of one CTA shape; one TMA descriptor per scan (of its pack buffer, in its
+  // group's form)
+  bool slab = false;
+  SlabLaunch slab_launch{};
+  CUtensorMap *tmaps_d = nullptr;
   int launches = 0;         // kernel launches of the last enqueue_outer
   Batch() = default;
   Batch(const Batch &) = delete;

@@ -109,6 +109,14 @@ struct ScanDev {
   int *bp_cnt;                 // [ntiles]
   int bp_split;                // CTAs per tile (>= 1)
   float4 *pack;                // [max(2*n*n, nbins)] fan/ray plans: a group's projector inputs, interleaved
+  // slab forward projector (fan / ray plans with slab tables): the plan's
+  // CTA shape and tables, and the TMA descriptor of this scan's pack buffer
+  // (lead scans: one float, float2 or float4 per pixel, row-major rows then
+  // transposed rows)
+  int slab_views, slab_rays, slab_rows, slab_wbox, slab_nslab, slab_ndb;
+  const uint4 *slab_cta;
+  const int16_t *slab_wlo;
+  const CUtensorMap *tmap;
   // scans of a batch that share this scan's plan and are projected together
   // with it: nmem members (scan indices, this one first) on the lead; 0 on
   // the others, which get no projector CTAs of their own
@@ -134,6 +142,15 @@ struct Launch {
   int flag;                      // kernel-specific (median this iteration, first pass, ...)
   int group;                     // projector launches: largest group of scans sharing a plan
   int tr;                        // forward projection: the scans' pack buffers hold transposed inputs
+};
+
+// Launch shape of the slab forward projector over a batch whose plans all
+// have slab tables of one CTA shape: threads per CTA, and dynamic shared
+// memory per group form (index 0: three or four members, float4; 1: a scan
+// alone, float; 2: a pair, float2), the largest over the batch's scans.
+struct SlabLaunch {
+  int threads;
+  size_t smem[3];
 };
 
 __device__ __forceinline__ int find_scan(const int *prefix, int nscans, int cta) {

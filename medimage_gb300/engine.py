@@ -77,6 +77,11 @@ class _PlanStats(C.Structure):
         ("fp_rays_per_thread", C.c_int32),
         ("bp_runs", C.c_int64),
         ("nz", C.c_int32),
+        ("slab_views", C.c_int32),
+        ("slab_rays", C.c_int32),
+        ("slab_rows", C.c_int32),
+        ("slab_wbox", C.c_int32),
+        ("slab_fallback_ctas", C.c_int32),
     ]
 
 
@@ -105,6 +110,7 @@ class _ServerStats(C.Structure):
         ("slices_per_s", C.c_double),
         ("busy_s", C.c_double),
         ("peak_state_bytes", C.c_size_t),
+        ("psnr_stops", C.c_int64),
     ]
 
 
@@ -116,6 +122,7 @@ SIGNATURES = {
     "at_plan_create_fan": ([C.POINTER(_FanGeom), C.POINTER(C.c_void_p)], C.c_int),
     "at_plan_create_fan_ex": ([C.POINTER(_FanGeom), C.c_int32, C.POINTER(C.c_void_p)], C.c_int),
     "at_plan_create_goldnc": ([C.POINTER(C.c_void_p)], C.c_int),
+    "at_plan_set_forward_variant": ([C.c_void_p, C.c_int32, C.c_int32, C.c_int32], C.c_int),
     "at_rowaction_create": ([C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)], C.c_int),
     "at_rowaction_destroy": ([C.c_void_p], None),
     "at_rowaction_segments": ([C.c_void_p, C.POINTER(C.c_int64)], C.c_int),
@@ -166,6 +173,10 @@ SIGNATURES = {
     "at_server_destroy": ([C.c_void_p], None),
     "at_server_submit": ([C.c_void_p, C.c_void_p, _fp, C.c_int32, C.c_double, C.POINTER(C.c_int64)], C.c_int),
     "at_server_run": ([C.c_void_p, C.c_double], C.c_int),
+    "at_server_submit_psnr": ([C.c_void_p, C.c_void_p, _fp, C.c_int32, C.c_double, _fp, C.c_double, C.c_double,
+                               C.POINTER(C.c_int64)], C.c_int),
+    "at_server_result_info": ([C.c_void_p, C.c_int64, C.POINTER(C.c_int32), C.POINTER(C.c_double),
+                               C.POINTER(C.c_int32)], C.c_int),
     "at_server_result": ([C.c_void_p, C.c_int64, _fp, _fp, C.POINTER(C.c_double), C.POINTER(C.c_double)], C.c_int),
     "at_server_get_stats": ([C.c_void_p, C.POINTER(_ServerStats)], C.c_int),
     # GoldenC drop-in (include/goldnc.h)
@@ -420,6 +431,14 @@ class Plan:
         except Exception:
             pass
 
+    def set_forward_variant(self, views: int = 0, rays: int = 0, rows: int = 0) -> None:
+        """Pin the forward projector: (0, 0, 0) the L1 walk, else the slab
+        projector with that CTA shape and slab height (bitwise the same sums)."""
+        _check("at_plan_set_forward_variant", lib().at_plan_set_forward_variant(self._h, views, rays, rows))
+        st = _PlanStats()
+        _check("at_plan_get_stats", lib().at_plan_get_stats(self._h, C.byref(st)))
+        self.stats = {k: getattr(st, k) for k, _ in _PlanStats._fields_}
+
     def trace_ray(self, view: int, det: int):
         cap = 4 * 8192
         pix = np.zeros(cap, np.int32)
@@ -490,6 +509,43 @@ class ProjSet:
     def back_dev(self, d_sinos, d_imgs, stream: int = 0) -> None:
         _check("at_projset_back", lib().at_projset_back(self._h, self._ptrs(d_sinos), self._ptrs(d_imgs),
                                                         C.c_void_p(stream)))
+
+    def _host_call(self, forward: bool, arrays):
+        if len(arrays) != len(self.plans):
+            raise ValueError(f"{len(arrays)} arrays for {len(self.plans)} plans")
+        L = lib()
+        ins, outs, res, held = [], [], [], []
+        try:
+            for p, a in zip(self.plans, arrays):
+                shape_in, shape_out = (p.img_shape, p.sino_shape) if forward else (p.sino_shape, p.img_shape)
+                a = np.ascontiguousarray(a, np.float32)
+                if a.shape != shape_in:
+                    raise ValueError(f"array shape {a.shape}, plan expects {shape_in}")
+                out = np.zeros(shape_out, np.float32)
+                di, do = C.c_void_p(), C.c_void_p()
+                _check("at_dev_alloc", L.at_dev_alloc(C.byref(di), a.nbytes))
+                held.append(di)
+                _check("at_dev_alloc", L.at_dev_alloc(C.byref(do), out.nbytes))
+                held.append(do)
+                _check("at_memcpy_h2d", L.at_memcpy_h2d(di, a.ctypes.data, a.nbytes, None))
+                ins.append(di.value)
+                outs.append(do.value)
+                res.append(out)
+            (self.forward_dev if forward else self.back_dev)(ins, outs)
+            for d, out in zip(outs, res):
+                _check("at_memcpy_d2h", L.at_memcpy_d2h(out.ctypes.data, C.c_void_p(d), out.nbytes, None))
+            _check("at_stream_sync", L.at_stream_sync(None))
+        finally:
+            for d in held:
+                L.at_dev_free(d)
+        return res
+
+    def forward(self, imgs):
+        """Host arrays in and out (device copies made and freed here)."""
+        return self._host_call(True, imgs)
+
+    def back(self, sinos):
+        return self._host_call(False, sinos)
 
 
 class Solver:
@@ -623,6 +679,27 @@ class Server:
                                                           C.byref(rid)))
         self._plans[rid.value] = plan
         return rid.value
+
+    def submit_psnr(self, plan: Plan, sino: np.ndarray, iter_alt: int, ref: np.ndarray, target_psnr_db: float,
+                    arrival_s: float = 0.0, peak: float = 0.0) -> int:
+        """A request with a quality stop: it finishes once PSNR(f, ref) (on the
+        GPU after every outer iteration) reaches target_psnr_db, or after
+        iter_alt outer iterations."""
+        sino = np.ascontiguousarray(sino, np.float32)
+        ref = np.ascontiguousarray(ref, np.float32)
+        if ref.shape != plan.img_shape:
+            raise ValueError(f"reference shape {ref.shape}, plan expects {plan.img_shape}")
+        rid = C.c_int64()
+        _check("at_server_submit_psnr", lib().at_server_submit_psnr(self._h, plan.handle, sino, iter_alt, arrival_s,
+                                                                    ref, target_psnr_db, peak, C.byref(rid)))
+        self._plans[rid.value] = plan
+        return rid.value
+
+    def result_info(self, rid: int) -> dict:
+        it, ps, stop = C.c_int32(), C.c_double(), C.c_int32()
+        _check("at_server_result_info", lib().at_server_result_info(self._h, rid, C.byref(it), C.byref(ps),
+                                                                    C.byref(stop)))
+        return {"iterations": it.value, "psnr_db": ps.value, "stopped_by_psnr": bool(stop.value)}
 
     def run(self, max_seconds: float = 0.0) -> None:
         _check("at_server_run", lib().at_server_run(self._h, max_seconds))

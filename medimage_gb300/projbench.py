@@ -92,7 +92,10 @@ def main() -> None:
                           "l2": "warm" if args.warm else "flushed",
                           "launch_ms": round(ms, 5), "gsegs_per_s": round(G * S / (ms / 1e3) / 1e9, 2),
                           "algorithmic_bytes": nbytes, "gbs": round(nbytes / (ms / 1e3) / 1e9, 1),
-                          "segments": S, "rays": R, "pixels": P}))
+                          "segments": S, "rays": R, "pixels": P,
+                          "variant": {k: plan.stats[k] for k in ("fp_rays_per_thread", "slab_views", "slab_rays",
+                                                                 "slab_rows", "slab_wbox", "slab_fallback_ctas")
+                                      if k in plan.stats}}))
     if pset is not None:
         pset.close()
     for p in bufs.values():

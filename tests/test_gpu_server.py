@@ -85,3 +85,53 @@ def test_server_mixes_slices_and_cone_volumes(engine, oracle):
         assert f_mix.shape == p.img_shape
         np.testing.assert_array_equal(f_mix, f_one)
         np.testing.assert_array_equal(v_mix, v_one)
+
+
+def test_server_quality_stop(engine, oracle):
+    """Requests with a PSNR target (measured on the GPU after every outer
+    iteration against the request's reference image) stop at the first
+    iteration that reaches it; a request stops at the same iteration and with
+    the same image alone and in a mix (bitwise), within 1e-6 of a solver run of
+    that many iterations, and the measured PSNR agrees with numpy's."""
+    G = engine.FanGeometry.covering
+    geoms = [G(64, 3.0, 90, 128), G(96, 2.0, 120, 160)]
+    plans = [engine.Plan.fan(g) for g in geoms]
+    reqs = []
+    for i in range(6):
+        g, p = geoms[i % 2], plans[i % 2]
+        ph = engine.phantom.ellipse_phantom(g.n, seed=500 + i, n_random=3)
+        clean = oracle.fan_A(oracle.fan_from_engine(g), ph.astype(np.float64))
+        sino = engine.phantom.poisson_sinogram(clean, 1e4, 600 + i)
+        target = 22.0 if i < 4 else 99.0  # the last two never reach theirs: iter_alt ends them
+        reqs.append((p, sino, 8, ph, target, 0.001 * i))
+
+    def serve(subset, slots):
+        srv = engine.Server(hbm_budget_bytes=1 << 34, max_active=slots)
+        ids = [srv.submit_psnr(p, s, it, ph, tgt, arr) for (p, s, it, ph, tgt, arr) in subset]
+        srv.run()
+        out = [(srv.result(i)[:2], srv.result_info(i)) for i in ids]
+        st = srv.stats()
+        srv.close()
+        return out, st
+
+    mix, st = serve(reqs, 4)
+    assert st["completed"] == len(reqs)
+    assert st["psnr_stops"] == sum(1 for (_, _, _, _, tgt, _), (_, info) in zip(reqs, mix) if info["stopped_by_psnr"])
+    for k, (req, ((f, v), info)) in enumerate(zip(reqs, mix)):
+        p, s, it, ph, tgt, _ = req
+        if tgt < 50:
+            assert info["stopped_by_psnr"] and info["iterations"] < it and info["psnr_db"] >= tgt
+        else:
+            assert not info["stopped_by_psnr"] and info["iterations"] == it and info["psnr_db"] < tgt
+        assert abs(info["psnr_db"] - engine.phantom.psnr(f, ph)) < 1e-6
+        (fa, va), ia = serve([req], 1)[0][0]
+        assert ia == info
+        np.testing.assert_array_equal(fa, f)
+        np.testing.assert_array_equal(va, v)
+        solver = engine.Solver([p], engine.Params(iter_alt=info["iterations"]))
+        solver.set_sino(0, s)
+        solver.run()
+        fs, vs = solver.get(0)
+        solver.close()
+        assert np.linalg.norm(fs - f) <= 1e-6 * np.linalg.norm(fs)
+        assert np.linalg.norm(vs - v) <= 1e-6 * np.linalg.norm(vs)

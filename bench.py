@@ -395,7 +395,7 @@ def run_ours(args):
         cone = run_cone_c4(mg, st, tstream) if args.cone else None
         c3 = run_batched_c3(mg, st, tstream) if args.c3 else None
         parity = finish_parity(mg, spec, par_gpu, ora, phantoms[0], sinos[0]) if args.parity else None
-        serving = run_serving(mg, args.serve_requests) if args.serve_requests > 0 else None
+        serving = run_serving(mg, args.serve_requests, target_db=args.serve_psnr) if args.serve_requests > 0 else None
         cpu = cpu_baseline(spec, sinos[0], args.cpu_outer) if not args.no_cpu else None
         openmp = run_openmp_equal_psnr(mg, st, tstream, batch=8) if not args.no_cpu else None
         goldnc = run_goldnc_native(mg) if not args.no_cpu else None
@@ -511,13 +511,17 @@ def finish_parity(mg, spec, gpu, ora, phantom, sino):
     return block
 
 
-def run_serving(mg, n_requests: int, seed: int = 5):
+def run_serving(mg, n_requests: int, seed: int = 5, target_db: float = 0.0):
     """C5-style serving sample: seeded requests with Poisson arrivals, served by
     the continuous-batching server and again one request at a time.  The mix is
     C5's: 256^2/512^2 slices with 360-720 views and 512-888 detectors, 1024^2
     slices with 1440 views x 1536 detectors (about 22 %), and every tenth
     request a 256^3 cone-beam volume with 360 projections of 384 x 512 cells;
-    20-50 outer iterations each."""
+    20-50 outer iterations each.  With target_db > 0 every request carries a
+    quality stop (its phantom as reference, PSNR measured on the GPU after each
+    outer iteration): it finishes at the first iteration reaching target_db,
+    or after its iteration count.  Both forms stop each request at the same
+    iteration with the same image (equal PSNR by construction)."""
     rng = np.random.default_rng(np.random.PCG64(seed))
     G = mg.FanGeometry.covering
     small = [G(256, 1.0, 360, 512), G(256, 1.0, 720, 888), G(512, 0.75, 720, 888), G(512, 0.75, 360, 512)]
@@ -555,23 +559,32 @@ def run_serving(mg, n_requests: int, seed: int = 5):
     arrivals = np.concatenate([[0.0], np.cumsum(gaps[:-1])])
     out = {}
     results = {}
+    infos = {}
     for name, slots in (("continuous", 64), ("one_at_a_time", 1)):
         srv = mg.Server(hbm_budget_bytes=150 << 30, max_active=slots)
-        ids = [srv.submit(p, s, it, float(a)) for (p, s, it, _), a in zip(reqs, arrivals)]
+        if target_db > 0:
+            ids = [srv.submit_psnr(p, s, it, ph, target_db, float(a)) for (p, s, it, ph), a in zip(reqs, arrivals)]
+        else:
+            ids = [srv.submit(p, s, it, float(a)) for (p, s, it, _), a in zip(reqs, arrivals)]
         srv.run()
         st = srv.stats()
         res = [srv.result(i) for i in ids]
+        infos[name] = [srv.result_info(i) for i in ids]
         results[name] = res
         out[name] = {"p50_latency_s": round(st["p50_latency_s"], 4), "p99_latency_s": round(st["p99_latency_s"], 4),
                      "slices_per_s": round(st["slices_per_s"], 4), "rounds": st["rounds"],
-                     "peak_state_gb": round(st["peak_state_bytes"] / 1e9, 3)}
+                     "peak_state_gb": round(st["peak_state_bytes"] / 1e9, 3), "psnr_stops": st["psnr_stops"]}
         srv.close()
     same = all(np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
                for a, b in zip(results["continuous"], results["one_at_a_time"]))
+    same_iters = [a["iterations"] for a in infos["continuous"]] == [b["iterations"] for b in infos["one_at_a_time"]]
     psnr = [mg.phantom.psnr(r[0], q[3]) for r, q in zip(results["continuous"], reqs)]
     out.update({"requests": n_requests, "mix": "C5: 256^2/512^2 slices, ~22% 1024^2 (1440x1536), every tenth a "
                                                 "256^3 cone volume (360 x 384 x 512)",
                 "iterations": "20-50 outer per request", "budget_gb": 150,
+                "quality_stop_psnr_db": target_db if target_db > 0 else None,
+                "iterations_run_median": float(np.median([a["iterations"] for a in infos["continuous"]])),
+                "same_stop_iteration_alone_vs_mix": bool(same_iters),
                 "results_identical_alone_vs_mix": bool(same), "psnr_db_median": round(float(np.median(psnr)), 3),
                 "speedup_slices_per_s": round(out["continuous"]["slices_per_s"] /
                                               max(out["one_at_a_time"]["slices_per_s"], 1e-12), 3)})
@@ -940,6 +953,10 @@ def main():
     ap.add_argument("--cpu-outer", type=int, default=1, help="outer iterations in the CPU baseline sample")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--serve-requests", type=int, default=12, help="requests in the serving sample (0 = skip)")
+    ap.add_argument("--serve-psnr", type=float, default=30.0,
+                    help="quality stop of every serving request (dB against its phantom; 0 = none)")
+    ap.add_argument("--serve-only", action="store_true",
+                    help="only the serving sample (its own JSON line; for long C5 runs)")
     ap.add_argument("--no-variants", dest="variants", action="store_false", help="skip the linear-mode variant")
     ap.add_argument("--no-cone", dest="cone", action="store_false", help="skip the C4 cone-beam projector sample")
     ap.add_argument("--no-c3", dest="c3", action="store_false", help="skip the C3 batched-versus-plain sample")
@@ -948,6 +965,10 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.serve_only:
+        import medimage_gb300 as mg
+
+        print(json.dumps({"serving": run_serving(mg, args.serve_requests, target_db=args.serve_psnr)}))
     else:
         run_ours(args)
 

@@ -872,7 +872,9 @@ cudaError_t launch_fp_single(const Launch &L, const Plan &p, int rpt, void *scra
     CUtensorMap *dmap = reinterpret_cast<CUtensorMap *>(reinterpret_cast<char *>(scratch) +
                                                         fp_single_scratch_bytes(p) - sizeof(CUtensorMap));
     CUtensorMap hmap;
-    if (encode_pack_tmap(&hmap, copies, n, 1, p.slab.wbox, p.slab.rows)) return cudaErrorInvalidValue;
+    // (a descriptor the driver refuses reads as "not supported", a launch
+    // configuration it refuses as "invalid argument")
+    if (encode_pack_tmap(&hmap, copies, n, 1, p.slab.wbox, p.slab.rows)) return cudaErrorNotSupported;
     cudaError_t e = cudaMemcpyAsync(dmap, &hmap, sizeof(hmap), cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return e;
     Lt.single.tmap = dmap;
@@ -1010,7 +1012,13 @@ int autotune_fan(Plan &p, cudaStream_t st) {
     if ((rc = build_slab_tables(p, shapes[i][0], shapes[i][1], shapes[i][2], st))) return rc;
     if (!p.slab.ok) continue;
     float ms = 0.f;
-    if ((rc = time_it(p.fp_rpt, ms))) return rc;
+    if (time_it(p.fp_rpt, ms)) {
+      // a shape the device refuses (shared memory, descriptor): skip it; a
+      // fault would be sticky and fail the next call
+      cudaGetLastError();
+      AT_CUDA_TRY(cudaStreamSynchronize(st));
+      continue;
+    }
     if (ms < best) {
       best = ms;
       pick = i;

@@ -359,14 +359,28 @@ size_t slab_smem_bytes(int G, int rows, int wbox) {
 }
 
 namespace {
+// Raises the kernel's dynamic shared memory limit to what a launch needs
+// (once per size; the limit is the device's opt-in maximum less the kernel's
+// static shared memory).  Returns cudaErrorInvalidValue for a size beyond it.
 template <int G>
 cudaError_t launch_slab_g(const Launch &L, int nctas, int threads, size_t smem, cudaStream_t st) {
-  static std::once_flag once;
-  static cudaError_t attr = cudaSuccess;
-  std::call_once(once, [] {
-    attr = cudaFuncSetAttribute(fan_fp_slab_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-  });
-  if (attr != cudaSuccess) return attr;
+  static std::mutex mu;
+  static size_t granted = 48 * 1024;  // every kernel may take 48 KB without opting in
+  if (smem > granted) {
+    std::lock_guard<std::mutex> lk(mu);
+    if (smem > granted) {
+      int dev = 0, optin = 0;
+      cudaError_t e = cudaGetDevice(&dev);
+      if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+      cudaFuncAttributes fa{};
+      if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, fan_fp_slab_kernel<G>);
+      if (e != cudaSuccess) return e;
+      if (smem + fa.sharedSizeBytes > (size_t)optin) return cudaErrorInvalidValue;
+      e = cudaFuncSetAttribute(fan_fp_slab_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+      granted = smem;
+    }
+  }
   fan_fp_slab_kernel<G><<<nctas, threads, smem, st>>>(L);
   return cudaGetLastError();
 }

@@ -1,6 +1,7 @@
 """Time the forward and back projectors alone on one workload geometry.
 
     python -m medimage_gb300.projbench [--config c1|c2|c4] [--n N] [--reps N] [--which fp,bp] [--group G]
+                                       [--variant l1|views,rays,rows]
 
 Prints one JSON line per projector: average launch time (CUDA events on the
 launching stream around each launch, L2 flushed before each unless --warm), algorithmic bytes per launch (forward 4 S + 4 R, back
@@ -30,6 +31,9 @@ def main() -> None:
     ap.add_argument("--which", default="fp,bp")
     ap.add_argument("--group", type=int, default=1, help="images projected together (2D plans)")
     ap.add_argument("--warm", action="store_true", help="no L2 flush between timed launches")
+    ap.add_argument("--variant", default="",
+                    help="forward projector of 2D plans: 'l1', or views,rays,rows of the slab projector "
+                         "(default: the autotuner's choice)")
     args = ap.parse_args()
     if args.config == "c4":
         spec = configs.c4(n=args.n, nz=args.n)
@@ -39,6 +43,9 @@ def main() -> None:
     else:
         spec = getattr(configs, args.config)()
         plan = engine.Plan.fan(spec.geom)
+        if args.variant:
+            plan.set_forward_variant(*([0, 0, 0] if args.variant == "l1" else
+                                       [int(x) for x in args.variant.split(",")]))
         img = phantom.ellipse_phantom(plan.n, seed=spec.seed, n_random=spec.n_random)
         names = ("fan_fp_kernel", "fan_bp_kernel")
     L = engine.lib()

@@ -92,18 +92,34 @@ def test_server_quality_stop(engine, oracle):
     iteration against the request's reference image) stop at the first
     iteration that reaches it; a request stops at the same iteration and with
     the same image alone and in a mix (bitwise), within 1e-6 of a solver run of
-    that many iterations, and the measured PSNR agrees with numpy's."""
+    that many iterations, and the measured PSNR agrees with numpy's.  Each
+    target is set from the request's own PSNR trajectory (a solver stepped one
+    outer iteration at a time), so the expected stop iteration is known."""
     G = engine.FanGeometry.covering
     geoms = [G(64, 3.0, 90, 128), G(96, 2.0, 120, 160)]
     plans = [engine.Plan.fan(g) for g in geoms]
-    reqs = []
+    iters = 8
+    reqs, expect = [], []
     for i in range(6):
         g, p = geoms[i % 2], plans[i % 2]
         ph = engine.phantom.ellipse_phantom(g.n, seed=500 + i, n_random=3)
         clean = oracle.fan_A(oracle.fan_from_engine(g), ph.astype(np.float64))
         sino = engine.phantom.poisson_sinogram(clean, 1e4, 600 + i)
-        target = 22.0 if i < 4 else 99.0  # the last two never reach theirs: iter_alt ends them
-        reqs.append((p, sino, 8, ph, target, 0.001 * i))
+        sv = engine.Solver([p], engine.Params(iter_alt=iters))
+        sv.set_sino(0, sino)
+        sv.reset()
+        traj = []
+        for _ in range(iters):
+            sv.step(1)
+            traj.append(engine.phantom.psnr(sv.get(0)[0], ph))
+        sv.close()
+        if i < 4:  # halfway between the PSNR after 3 and after 4 outer iterations
+            target = 0.5 * (traj[2] + traj[3]) if traj[3] > traj[2] else traj[3] - 1e-3
+            stop = next(k + 1 for k, t in enumerate(traj) if t >= target)
+        else:  # unreachable: iter_alt ends the request
+            target, stop = max(traj) + 5.0, iters
+        reqs.append((p, sino, iters, ph, target, 0.001 * i))
+        expect.append(stop)
 
     def serve(subset, slots):
         srv = engine.Server(hbm_budget_bytes=1 << 34, max_active=slots)
@@ -116,14 +132,13 @@ def test_server_quality_stop(engine, oracle):
 
     mix, st = serve(reqs, 4)
     assert st["completed"] == len(reqs)
-    assert st["psnr_stops"] == sum(1 for (_, _, _, _, tgt, _), (_, info) in zip(reqs, mix) if info["stopped_by_psnr"])
-    for k, (req, ((f, v), info)) in enumerate(zip(reqs, mix)):
+    assert st["psnr_stops"] == sum(1 for _, info in mix if info["stopped_by_psnr"])
+    for req, stop, ((f, v), info) in zip(reqs, expect, mix):
         p, s, it, ph, tgt, _ = req
-        if tgt < 50:
-            assert info["stopped_by_psnr"] and info["iterations"] < it and info["psnr_db"] >= tgt
-        else:
-            assert not info["stopped_by_psnr"] and info["iterations"] == it and info["psnr_db"] < tgt
+        assert info["iterations"] == stop
+        assert info["stopped_by_psnr"] == (stop < it)
         assert abs(info["psnr_db"] - engine.phantom.psnr(f, ph)) < 1e-6
+        assert (info["psnr_db"] >= tgt) == info["stopped_by_psnr"] or stop == it
         (fa, va), ia = serve([req], 1)[0][0]
         assert ia == info
         np.testing.assert_array_equal(fa, f)

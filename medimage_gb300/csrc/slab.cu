@@ -262,28 +262,47 @@ __global__ void __launch_bounds__(512, 2) fan_fp_slab_kernel(const Launch L) {
         const int wlo = __ldg(wlo_row + s);
         int off = (u - row0) * WB + (w - wlo);
         int uleft = su > 0 ? row0 + SH - u : u - row0 + 1;  // u steps before the ray leaves the slab
-        while (true) {
+        // Word by word: the decision bits say how many of the word's segments
+        // stay in the slab (up to and including the uleft-th step along u),
+        // so each run is walked without per-step exit checks.
+        while (k < nseg && uleft > 0) {
           const int navail = min(32 - b, nseg - k);
-          uint32_t wb = word >> b;
-          int t = 0;
-          while (t < navail) {
-            const bool bx = wb & 1u;
-            wb >>= 1;
+          const uint32_t wb = word >> b;
+          const uint32_t vmask = navail == 32 ? 0xffffffffu : ((1u << navail) - 1u);
+          uint32_t um = (ubit ? wb : ~wb) & vmask;  // the steps along u among them
+          const int cu = __popc(um);
+          int nrun = navail;
+          if (cu >= uleft) {  // leaves the slab at its uleft-th u step: find that bit
+            int need = uleft, pos = 0;
+#pragma unroll
+            for (int sh = 16; sh > 0; sh >>= 1) {
+              const int c = __popc(um & ((1u << sh) - 1u));
+              if (c < need) {
+                need -= c;
+                um >>= sh;
+                pos += sh;
+              }
+            }
+            nrun = pos + 1;
+            uleft = 0;
+          } else {
+            uleft -= cu;
+          }
+          uint32_t wr = wb;
+          for (int t = 0; t < nrun; t++) {
+            const bool bx = wr & 1u;
+            wr >>= 1;
             const float nx = fmaf(cx, lx, ax), ny = fmaf(cy, ly, ay);
             const float cur = bx ? nx : ny;
             const float wt = cur - prev;
             prev = cur;
             fma_elem<G>(part, wt, tile[off]);
-            const bool us = (uint32_t)bx == ubit;
-            off += us ? du : dw;
-            uleft -= us ? 1 : 0;
+            off += ((uint32_t)bx == ubit) ? du : dw;
             cx += bx ? 1.f : 0.f;
             cy += bx ? 0.f : 1.f;
-            t++;
-            if (uleft == 0) break;
           }
-          k += t;
-          b += t;
+          k += nrun;
+          b += nrun;
           if (b == 32 || k == nseg) {  // a word ends: fold its sum (as the L1 kernel does)
 #pragma unroll
             for (int m = 0; m < G; m++) {
@@ -295,7 +314,6 @@ __global__ void __launch_bounds__(512, 2) fan_fp_slab_kernel(const Launch L) {
               if (k < nseg) word = __ldg(wp + (size_t)(k >> 5) * kRayBlock);
             }
           }
-          if (k == nseg || uleft == 0) break;
         }
         if (k < nseg) {  // stepped out through the far edge: into the next slab
           const int lrow = su > 0 ? SH : -1;

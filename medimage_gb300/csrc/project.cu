@@ -95,10 +95,12 @@ __global__ void __launch_bounds__(256) fp_pack_kernel(const Launch L, int bins) 
 }
 
 // RPT rays per thread; G scans per walk: 1, or a group's 2 or 4 members
-// gathered as one float2 / float4 (three members take the float4 form)
+// gathered as one float2 / float4 (three members take the float4 form).
+// `unit` is the CTA's index in the ordinary launch (blockIdx.x), or the work
+// unit a persistent CTA pulled from the queue.
 template <int RPT, int G>
-__global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
-  const int scan = L.scans ? find_scan(L.prefix, L.nscans, blockIdx.x) : 0;
+__device__ __forceinline__ void fan_fp_body(const Launch &L, const int unit) {
+  const int scan = L.scans ? find_scan(L.prefix, L.nscans, unit) : 0;
   const ScanDev &S = scan_of(L, scan);
   const int nm = L.scans ? S.nmem : 1;
   const ScanDev *M[G];
@@ -113,7 +115,7 @@ __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
   if (!any) return;
   const int cta0 = L.scans ? __ldg(L.prefix + scan) : 0;
   const int ncta = L.scans ? __ldg(L.prefix + scan + 1) - cta0 : gridDim.x;
-  const int local_cta = blockIdx.x - cta0;
+  const int local_cta = unit - cta0;
   constexpr int kWarpsPerBlock = 4 / RPT;  // warps per 128-ray bit block
   const int lane = threadIdx.x & 31;
   const int lw = local_cta * (int)(blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -312,6 +314,17 @@ __global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
   }
 }
 
+template <int RPT, int G>
+__global__ void __launch_bounds__(128) fan_fp_kernel(const Launch L) {
+  fan_fp_body<RPT, G>(L, blockIdx.x);
+}
+
+// the same work from a queue, over a grid of resident CTAs
+template <int RPT, int G>
+__global__ void __launch_bounds__(128) fan_fp_queue_kernel(const Launch L) {
+  persistent_loop(L, [&](int unit) { fan_fp_body<RPT, G>(L, unit); });
+}
+
 
 // ---------------------------------------------------------------------------
 // fan-beam back projection (gather over tile runs)
@@ -368,10 +381,10 @@ __global__ void __launch_bounds__(256) sino_absmax_kernel(const Launch L) {
 }
 
 template <int G, int C>
-__device__ __forceinline__ void fan_bp_body(const Launch &L) {
+__device__ __forceinline__ void fan_bp_body(const Launch &L, const int unit) {
   constexpr int kStride = bp_copy_stride<C>();  // one copy
   constexpr int kMemStride = C * kStride;       // one member
-  const int scan = L.scans ? find_scan(L.prefix, L.nscans, blockIdx.x) : 0;
+  const int scan = L.scans ? find_scan(L.prefix, L.nscans, unit) : 0;
   const ScanDev &S = scan_of(L, scan);
   const int nm = L.scans ? S.nmem : 1;
   const ScanDev *M[G];
@@ -386,7 +399,7 @@ __device__ __forceinline__ void fan_bp_body(const Launch &L) {
   if (!any) return;
   const int cta0 = L.scans ? __ldg(L.prefix + scan) : 0;
   const int ncta = L.scans ? __ldg(L.prefix + scan + 1) - cta0 : gridDim.x;
-  const int local_cta = blockIdx.x - cta0;
+  const int local_cta = unit - cta0;
   const int ntiles = S.ntiles_y * S.ntiles_y;
   // CTA = (split, tile): split s walks view blocks [s*nvb/split, (s+1)*nvb/split)
   const int tile = local_cta % ntiles, split = local_cta / ntiles;
@@ -582,20 +595,30 @@ __device__ __forceinline__ void fan_bp_body(const Launch &L) {
   }
 }
 
-__global__ void __launch_bounds__(256) fan_bp_kernel(const Launch L) { fan_bp_body<1, kBpCopies1>(L); }
+__global__ void __launch_bounds__(256) fan_bp_kernel(const Launch L) { fan_bp_body<1, kBpCopies1>(L, blockIdx.x); }
+__global__ void __launch_bounds__(256) fan_bp_queue_kernel(const Launch L) {
+  persistent_loop(L, [&](int unit) { fan_bp_body<1, kBpCopies1>(L, unit); });
+}
 // four CTAs per SM (at most 64 registers; some setup state spills, and the
 // walk's latency is hidden better than at three CTAs with 80: two outer
 // iterations of four C2 slices 52.8 -> 51.3 ms)
 __global__ void __launch_bounds__(256, 4) fan_bp_group_kernel(const Launch L) {
-  fan_bp_body<kGroupMax, kBpCopiesG>(L);
+  fan_bp_body<kGroupMax, kBpCopiesG>(L, blockIdx.x);
+}
+__global__ void __launch_bounds__(256, 4) fan_bp_group_queue_kernel(const Launch L) {
+  persistent_loop(L, [&](int unit) { fan_bp_body<kGroupMax, kBpCopiesG>(L, unit); });
 }
 // in a batch with groups, the scans alone and the pairs
-__global__ void __launch_bounds__(256, 3) fan_bp_small_kernel(const Launch L) {
-  const ScanDev &S = L.scans[find_scan(L.prefix, L.nscans, blockIdx.x)];
+__device__ __forceinline__ void fan_bp_small_body(const Launch &L, int unit) {
+  const ScanDev &S = L.scans[find_scan(L.prefix, L.nscans, unit)];
   if (S.nmem <= 1)
-    fan_bp_body<1, kBpCopiesG>(L);
+    fan_bp_body<1, kBpCopiesG>(L, unit);
   else
-    fan_bp_body<2, kBpCopiesG>(L);
+    fan_bp_body<2, kBpCopiesG>(L, unit);
+}
+__global__ void __launch_bounds__(256, 3) fan_bp_small_kernel(const Launch L) { fan_bp_small_body(L, blockIdx.x); }
+__global__ void __launch_bounds__(256, 3) fan_bp_small_queue_kernel(const Launch L) {
+  persistent_loop(L, [&](int unit) { fan_bp_small_body(L, unit); });
 }
 
 // ---------------------------------------------------------------------------
@@ -742,6 +765,31 @@ size_t slab_smem_bytes(int G, int rows, int wbox);
 int encode_pack_tmap(CUtensorMap *out, const void *pack, int n, int G, int wbox, int rows);
 cudaError_t launch_cone_bp(const Launch &L, int nctas, const Launch &Lpix, int pix_nctas, cudaStream_t st);
 
+// CTAs of `kernel` (with `threads` threads) resident on the whole device at
+// once: the grid of its persistent (queue) form
+template <typename K>
+int resident_ctas(K kernel, int threads) {
+  int nb = 0, dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, threads, 0) != cudaSuccess)
+    return 152;
+  return std::max(1, nb * sms);
+}
+
+// launches `kernel`, or its queue form `qkernel` over the resident CTAs when
+// the launch carries a work queue
+template <typename K>
+void launch_maybe_queued(K kernel, K qkernel, int &resident, const Launch &L, int nctas, int threads,
+                         cudaStream_t st) {
+  if (nctas <= 0) return;
+  if (L.queue) {
+    if (resident <= 0) resident = resident_ctas(qkernel, threads);
+    qkernel<<<std::min(nctas, resident), threads, 0, st>>>(L);
+  } else {
+    kernel<<<nctas, threads, 0, st>>>(L);
+  }
+}
+
 int fp_ctas(const ScanDev &S, int rpt) {
   if (S.kind == AT_GEOM_GOLDNC) return (kGcFpWarps + 3) / 4;
   if (S.kind == AT_GEOM_CONE) return cone_ctas(S);
@@ -779,11 +827,14 @@ cudaError_t launch_fp(const Launch &L, int kind, int rpt, int nctas, cudaStream_
   } else if (kind == AT_GEOM_CONE) {
     return launch_cone_fp(L, nctas, st);
   } else if (rpt == 4) {
-    fan_fp_kernel<4, 1><<<nctas, 128, 0, st>>>(L);
+    static int res = 0;
+    launch_maybe_queued(fan_fp_kernel<4, 1>, fan_fp_queue_kernel<4, 1>, res, L, nctas, 128, st);
   } else if (rpt == 2) {
-    fan_fp_kernel<2, 1><<<nctas, 128, 0, st>>>(L);
+    static int res = 0;
+    launch_maybe_queued(fan_fp_kernel<2, 1>, fan_fp_queue_kernel<2, 1>, res, L, nctas, 128, st);
   } else {
-    fan_fp_kernel<1, 1><<<nctas, 128, 0, st>>>(L);
+    static int res = 0;
+    launch_maybe_queued(fan_fp_kernel<1, 1>, fan_fp_queue_kernel<1, 1>, res, L, nctas, 128, st);
   }
   return cudaGetLastError();
 }
@@ -811,19 +862,12 @@ int launch_fp_group(const Launch &L, const Launch &Lpix, const Launch &L1, const
   }
   Launch Lg = L, Lg1 = L1, Lg2 = L2;
   Lg.tr = Lg1.tr = Lg2.tr = 1;
-  if (nctas > 0) {
-    fan_fp_kernel<1, kGroupMax><<<nctas, kFpGroupThreads, 0, st>>>(Lg);
-    n++;
-  }
-  if (nctas1 > 0) {
-    fan_fp_kernel<1, 1><<<nctas1, kFpGroupThreads, 0, st>>>(Lg1);
-    n++;
-  }
-  if (nctas2 > 0) {
-    fan_fp_kernel<1, 2><<<nctas2, kFpGroupThreads, 0, st>>>(Lg2);
-    n++;
-  }
-  return n;
+  static int res4 = 0, res1 = 0, res2 = 0;
+  launch_maybe_queued(fan_fp_kernel<1, kGroupMax>, fan_fp_queue_kernel<1, kGroupMax>, res4, Lg, nctas,
+                      kFpGroupThreads, st);
+  launch_maybe_queued(fan_fp_kernel<1, 1>, fan_fp_queue_kernel<1, 1>, res1, Lg1, nctas1, kFpGroupThreads, st);
+  launch_maybe_queued(fan_fp_kernel<1, 2>, fan_fp_queue_kernel<1, 2>, res2, Lg2, nctas2, kFpGroupThreads, st);
+  return n + (nctas > 0) + (nctas1 > 0) + (nctas2 > 0);
 }
 
 // out[p] = in[p] and out[n*n + y*n + x] = in[x*n + y] for an n x n image
@@ -911,17 +955,14 @@ int launch_fp_tr(const Launch &L, const Launch &Lpix, int rpt, int nctas, int pi
 int launch_bp_group(const Launch &L, const Launch &Lsino, const Launch &Lsmall, int nctas, int sino_nctas,
                     int small_nctas, cudaStream_t st) {
   int n = 2;
-  sino_absmax_kernel<<<L.nscans * kBpMaxParts, 256, 0, st>>>(L);
+  Launch La = L;  // the max |r| pass: one CTA per part, never queued
+  La.queue = nullptr;
+  sino_absmax_kernel<<<L.nscans * kBpMaxParts, 256, 0, st>>>(La);
   fp_pack_kernel<<<sino_nctas, 256, 0, st>>>(Lsino, 1);
-  if (nctas > 0) {
-    fan_bp_group_kernel<<<nctas, 256, 0, st>>>(L);
-    n++;
-  }
-  if (small_nctas > 0) {
-    fan_bp_small_kernel<<<small_nctas, 256, 0, st>>>(Lsmall);
-    n++;
-  }
-  return n;
+  static int resg = 0, ress = 0;
+  launch_maybe_queued(fan_bp_group_kernel, fan_bp_group_queue_kernel, resg, L, nctas, 256, st);
+  launch_maybe_queued(fan_bp_small_kernel, fan_bp_small_queue_kernel, ress, Lsmall, small_nctas, 256, st);
+  return n + (nctas > 0) + (small_nctas > 0);
 }
 
 // Lpix / pix_nctas: the same launch over pixel-pass CTAs, for kernels whose
@@ -934,8 +975,11 @@ cudaError_t launch_bp(const Launch &L, int kind, int nctas, cudaStream_t st, con
     sino_absmax_kernel<<<(L.scans ? L.nscans : 1) * kBpMaxParts, 256, 0, st>>>(L);
     return launch_cone_bp(L, nctas, *Lpix, pix_nctas, st);
   } else {
-    sino_absmax_kernel<<<(L.scans ? L.nscans : 1) * kBpMaxParts, 256, 0, st>>>(L);
-    fan_bp_kernel<<<nctas, 256, 0, st>>>(L);
+    Launch La = L;  // the max |r| pass: one CTA per part, never queued
+    La.queue = nullptr;
+    sino_absmax_kernel<<<(L.scans ? L.nscans : 1) * kBpMaxParts, 256, 0, st>>>(La);
+    static int res = 0;
+    launch_maybe_queued(fan_bp_kernel, fan_bp_queue_kernel, res, L, nctas, 256, st);
   }
   return cudaGetLastError();
 }

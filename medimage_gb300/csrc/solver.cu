@@ -168,10 +168,19 @@ Ctl make_ctl(const at_params &prm) {
 }
 
 // ---------------------------------------------------------------- Batch
+// Projector launches of fan-beam / ray-table batches run persistent: a grid of
+// the resident CTAs pulling work units from a queue (set to 0 at build time to
+// launch one CTA per unit instead; results are the same).
+#ifndef MEDIMG_PERSISTENT_BATCHES
+#define MEDIMG_PERSISTENT_BATCHES 1
+#endif
+
 Batch::~Batch() {
   cudaFree(scans_d);
   cudaFree(prefix_d);
   cudaFree(tmaps_d);
+  cudaFree(queue_d);
+  cudaFree(order_d);
 }
 
 int Batch::set(const ScanDev *scans, int n, int kind_, int rpt_, cudaStream_t st) {
@@ -274,10 +283,55 @@ int Batch::set(const ScanDev *scans, int n, int kind_, int rpt_, cudaStream_t st
   fp1_total = pref[FAM_FP1 * (n + 1) + n];
   fp2_total = pref[FAM_FP2 * (n + 1) + n];
   bps_total = pref[FAM_BPS * (n + 1) + n];
+  // work orders of the persistent projector launches: per family, the units
+  // of each scan in their natural order, scans by decreasing work per unit
+  // (segments ~ views x detectors x n), so the cheapest units come last
+  persistent = MEDIMG_PERSISTENT_BATCHES && (kind == AT_GEOM_FAN || kind == AT_GEOM_RAYS);
+  if (persistent) {
+    std::vector<int> order;
+    const int fams[5] = {FAM_FP, FAM_FP1, FAM_FP2, FAM_BP, FAM_BPS};
+    for (int f : fams) {
+      order_off[f] = (int)order.size();
+      std::vector<int> idx;
+      for (int s = 0; s < n; s++)
+        if (pref[f * (n + 1) + s + 1] > pref[f * (n + 1) + s]) idx.push_back(s);
+      auto density = [&](int s) {
+        const double units = pref[f * (n + 1) + s + 1] - pref[f * (n + 1) + s];
+        return (double)scans[s].nviews * scans[s].ndets * scans[s].n / units;
+      };
+      std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return density(a) > density(b); });
+      for (int s : idx)
+        for (int u = pref[f * (n + 1) + s]; u < pref[f * (n + 1) + s + 1]; u++) order.push_back(u);
+    }
+    if (!queue_d) {
+      AT_CUDA_TRY(cudaMalloc(&queue_d, 2 * sizeof(unsigned)));
+      AT_CUDA_TRY(cudaMemsetAsync(queue_d, 0, 2 * sizeof(unsigned), st));
+    }
+    if (order.size() > order_cap) {
+      cudaFree(order_d);
+      order_d = nullptr;
+      order_cap = std::max(order.size(), 2 * order_cap);
+      AT_CUDA_TRY(cudaMalloc(&order_d, sizeof(int) * order_cap));
+    }
+    if (!order.empty())
+      AT_CUDA_TRY(cudaMemcpyAsync(order_d, order.data(), sizeof(int) * order.size(), cudaMemcpyHostToDevice, st));
+  }
   // pageable sources: the copies are staged before cudaMemcpyAsync returns
   AT_CUDA_TRY(cudaMemcpyAsync(scans_d, scans, sizeof(ScanDev) * n, cudaMemcpyHostToDevice, st));
   AT_CUDA_TRY(cudaMemcpyAsync(prefix_d, pref.data(), sizeof(int) * pref.size(), cudaMemcpyHostToDevice, st));
   return AT_OK;
+}
+
+// L with family's CTA ranges and, for persistent projector families, its
+// work order (other families: no queue)
+Launch Batch::retarget(const Launch &L0, int family) const {
+  const Launch B = base_launch(family);
+  Launch L = L0;
+  L.prefix = B.prefix;
+  L.queue = B.queue;
+  L.order = B.order;
+  L.units = B.units;
+  return L;
 }
 
 Launch Batch::base_launch(int family) const {
@@ -288,23 +342,26 @@ Launch Batch::base_launch(int family) const {
   L.prefix = prefix_d + family * (nscans + 1);
   L.aux_buf = -1;
   L.group = (family == FAM_PIX || family == FAM_SINO) ? 1 : group;
+  const bool fp = family == FAM_FP || family == FAM_FP1 || family == FAM_FP2;
+  if (persistent && (family == FAM_BP || family == FAM_BPS || (fp && !slab))) {
+    L.queue = queue_d;
+    L.order = order_d + order_off[family];
+    const int totals[kFamilies] = {fp_total, pix_total, sino_total, bp_total, fp1_total, fp2_total, bps_total};
+    L.units = totals[family];
+  }
   return L;
 }
 
 int Batch::enqueue_fp(const Launch &L, cudaStream_t st) {
   if (group > 1) {  // interleave each group's inputs, then one walk per group
-    Launch Lp = L, L1 = L, L2 = L;
-    Lp.prefix = prefix_d + FAM_PIX * (nscans + 1);
-    L1.prefix = prefix_d + FAM_FP1 * (nscans + 1);
-    L2.prefix = prefix_d + FAM_FP2 * (nscans + 1);
+    const Launch Lp = retarget(L, FAM_PIX), L1 = retarget(L, FAM_FP1), L2 = retarget(L, FAM_FP2);
     const int nl = launch_fp_group(L, Lp, L1, L2, fp_total, pix_total, fp1_total, fp2_total,
                                    slab ? &slab_launch : nullptr, st);
     AT_CUDA_TRY(cudaGetLastError());
     if (nl < 0) return set_error(AT_ECUDA, "grouped forward projection launch failed");
     launches += nl;
   } else if (kind == AT_GEOM_FAN || kind == AT_GEOM_RAYS) {  // transpose each input, then walk
-    Launch Lp = L;
-    Lp.prefix = prefix_d + FAM_PIX * (nscans + 1);
+    const Launch Lp = retarget(L, FAM_PIX);
     const int nl = launch_fp_tr(L, Lp, rpt, fp_total, pix_total, slab ? &slab_launch : nullptr, st);
     AT_CUDA_TRY(cudaGetLastError());
     if (nl < 0) return set_error(AT_ECUDA, "forward projection launch failed");
@@ -318,15 +375,12 @@ int Batch::enqueue_fp(const Launch &L, cudaStream_t st) {
 
 int Batch::enqueue_bp(const Launch &L, cudaStream_t st) {
   if (group > 1) {  // max |r|, interleave each group's sinograms, then one run walk per group
-    Launch Ls = L, Lsm = L;
-    Ls.prefix = prefix_d + FAM_SINO * (nscans + 1);
-    Lsm.prefix = prefix_d + FAM_BPS * (nscans + 1);
+    const Launch Ls = retarget(L, FAM_SINO), Lsm = retarget(L, FAM_BPS);
     launches += launch_bp_group(L, Ls, Lsm, bp_total, sino_total, bps_total, st);
     AT_CUDA_TRY(cudaGetLastError());
     return AT_OK;
   }
-  Launch Lp = L;  // the per-pixel finishing pass of the cone-beam back projector
-  Lp.prefix = prefix_d + FAM_PIX * (nscans + 1);
+  const Launch Lp = retarget(L, FAM_PIX);  // the per-pixel finishing pass of the cone-beam back projector
   AT_CUDA_TRY(launch_bp(L, kind, bp_total, st, &Lp, pix_total));
   // max |r| pass + back projection (+ per-pixel finish for the cone beam)
   launches += kind == AT_GEOM_GOLDNC ? 1 : kind == AT_GEOM_CONE ? 3 : 2;

@@ -43,6 +43,14 @@ struct Batch {
   bool slab = false;
   SlabLaunch slab_launch{};
   CUtensorMap *tmaps_d = nullptr;
+  // persistent projector launches (fan beam and ray tables): a grid of
+  // resident CTAs pulls (scan, view block, ray block) / (scan, pixel tile)
+  // units from a queue, the units of the costlier scans first
+  bool persistent = false;
+  unsigned *queue_d = nullptr;  // [2]: next unit, CTAs done (left zero by the kernels)
+  int *order_d = nullptr;       // unit order of each projector family
+  size_t order_cap = 0;
+  int order_off[kFamilies] = {};
   int launches = 0;         // kernel launches of the last enqueue_outer
   Batch() = default;
   Batch(const Batch &) = delete;
@@ -50,6 +58,7 @@ struct Batch {
   ~Batch();
   int set(const ScanDev *scans, int n, int kind, int rpt, cudaStream_t st);
   Launch base_launch(int family) const;
+  Launch retarget(const Launch &L, int family) const;
   // one forward / back projection of every scan (L from base_launch(FAM_FP /
   // FAM_BP) with flow, stage and buffers set); scans sharing a plan are grouped
   int enqueue_fp(const Launch &L, cudaStream_t st);

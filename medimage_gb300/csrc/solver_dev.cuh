@@ -142,7 +142,41 @@ struct Launch {
   int flag;                      // kernel-specific (median this iteration, first pass, ...)
   int group;                     // projector launches: largest group of scans sharing a plan
   int tr;                        // forward projection: the scans' pack buffers hold transposed inputs
+  // persistent launches (projectors of a batch): a grid sized to the resident
+  // CTAs pulls work units (the CTA indices of the ordinary launch) from a
+  // queue; order[i] is the i-th unit handed out (all units of the costlier
+  // scans first), queue[0] the next position, queue[1] the CTAs done.  The
+  // last CTA to finish resets both, so the launch can be replayed.
+  unsigned *queue;
+  const int *order;
+  int units;
 };
+
+// Runs body(unit) for every unit of a persistent launch, one unit per CTA at a
+// time (the unit index stands for blockIdx.x of the ordinary launch).
+template <typename Body>
+__device__ __forceinline__ void persistent_loop(const Launch &L, Body body) {
+  __shared__ int s_unit;
+  while (true) {
+    __syncthreads();  // the previous unit's shared memory is free, s_unit read
+    if (threadIdx.x == 0) {
+      const unsigned i = atomicAdd(L.queue, 1u);
+      s_unit = i < (unsigned)L.units ? __ldg(L.order + i) : -1;
+    }
+    __syncthreads();
+    const int unit = s_unit;
+    if (unit < 0) break;
+    body(unit);
+  }
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(L.queue + 1, 1u) == gridDim.x - 1) {  // every CTA has stopped pulling
+      L.queue[0] = 0u;
+      L.queue[1] = 0u;
+      __threadfence();
+    }
+  }
+}
 
 // Launch shape of the slab forward projector over a batch whose plans all
 // have slab tables of one CTA shape: threads per CTA, and dynamic shared

@@ -953,7 +953,7 @@ def main():
     ap.add_argument("--cpu-outer", type=int, default=1, help="outer iterations in the CPU baseline sample")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--serve-requests", type=int, default=12, help="requests in the serving sample (0 = skip)")
-    ap.add_argument("--serve-psnr", type=float, default=30.0,
+    ap.add_argument("--serve-psnr", type=float, default=26.0,
                     help="quality stop of every serving request (dB against its phantom; 0 = none)")
     ap.add_argument("--serve-only", action="store_true",
                     help="only the serving sample (its own JSON line; for long C5 runs)")

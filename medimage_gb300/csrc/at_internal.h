@@ -87,6 +87,7 @@ struct Plan {
   // from the host libm as in the reference's rotate_2d)
   at_cone_geometry cone{};
   float2 *cone_trig_d = nullptr;
+  int cone_bp_views = 0;  // views per back-projection chunk (32-bit voxel sums cannot overflow)
   int64_t rays = 0, segments = 0, offgrid = 0, device_bytes = 0;
   int max_segments = 0;
   int fp_rpt = 1;  // rays per thread of the forward projector (autotuned)

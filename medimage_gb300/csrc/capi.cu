@@ -85,6 +85,7 @@ int project(const Plan &p, bool forward, const float *in, float *out, cudaStream
       carve_bp_scratch(L.single, p, (char *)scratch);
       L.single.bp_split = bp_split_for(p.ntiles, p.nvb);
     }
+    if (p.kind == AT_GEOM_CONE) L.chunks = (p.nviews + p.cone_bp_views - 1) / std::max(1, p.cone_bp_views);
     e = launch_bp(L, p.kind, bp_ctas(L.single), st, &L, pix_ctas(L.single));
     if (scratch) cudaFreeAsync(scratch, st);
   }

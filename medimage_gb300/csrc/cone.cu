@@ -221,6 +221,18 @@ __device__ __forceinline__ int64_t cone_bin_of(const ScanDev &S, int64_t i) {
   return ((int64_t)view * S.ndx + row) * S.ndy + col;
 }
 
+// the bin of work item i of the back projection's chunk of views [v0, v0+nv):
+// the same band order over those views only
+__device__ __forceinline__ int64_t cone_bin_of_chunk(const ScanDev &S, int64_t i, int v0, int nv) {
+  const int64_t full = (int64_t)kConeBandRows * S.ndy * nv;
+  const int64_t b = i / full, off = i - b * full;
+  const int rows_b = min(kConeBandRows, S.ndx - (int)b * kConeBandRows);
+  const int64_t per_view = (int64_t)rows_b * S.ndy;
+  const int view = v0 + (int)(off / per_view), r2 = (int)(off - (view - v0) * per_view);
+  const int row = (int)b * kConeBandRows + r2 / S.ndy, col = r2 % S.ndy;
+  return ((int64_t)view * S.ndx + row) * S.ndy + col;
+}
+
 // ---------------------------------------------------------------------------
 // forward
 // ---------------------------------------------------------------------------
@@ -286,39 +298,77 @@ __device__ __forceinline__ int cone_bp_sexp(const ScanDev &S) {
   return s_sexp;
 }
 
+// One chunk of views (L.chunk; S.bp_vchunk views each), rays in band order,
+// a grid-stride loop over the chunk's rays.  Each term w*r is rounded to an
+// integer below 2^22 (one FFMA, magic-number rounding) and added with a 32-bit
+// atomic into the chunk's accumulator; the chunk is short enough that no
+// voxel's sum can leave 32 bits (cone_bp_views_per_chunk), and the fold pass
+// moves it into the exact 64-bit sum before the next chunk.  Integer sums do
+// not depend on order, so the result is deterministic, and bitwise the same
+// as adding every term into 64 bits.
 __global__ void __launch_bounds__(kConeThreads) cone_bp_kernel(const Launch L) {
+  const int scan = L.scans ? find_scan(L.prefix, L.nscans, blockIdx.x) : 0;
+  const ScanDev &S = scan_of(L, scan);
+  if (!flow_active(S, L.flow)) return;
+  const int v0 = L.chunk * S.bp_vchunk;
+  if (v0 >= S.nviews) return;  // a scan with fewer chunks than the launch's largest
+  const int nv = min(S.bp_vchunk, S.nviews - v0);
+  const int cta0 = L.scans ? __ldg(L.prefix + scan) : 0;
+  const int ncta = L.scans ? __ldg(L.prefix + scan + 1) - cta0 : gridDim.x;
+  const int local_cta = blockIdx.x - cta0;
+  const int sexp = cone_bp_sexp(S);
+  const float scale = ldexpf(1.f, sexp);
+  const int64_t nitems = (int64_t)nv * S.ndets;
+  constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
+  constexpr int kMagicBits = 0x4B400000;
+  int *acc = S.bp_acc32;
+  auto none = [] {};
+  for (int64_t item = (int64_t)local_cta * kConeThreads + threadIdx.x; item < nitems;
+       item += (int64_t)ncta * kConeThreads) {
+    const int64_t ray = cone_bin_of_chunk(S, item, v0, nv);
+    const float r = S.buf[L.in_buf][ray];
+    if (r == 0.f) continue;
+    const float rs = r * scale;
+    ConeWalk w = cone_ray(S, ray);
+    if (w.empty) continue;
+    auto seg = [&](bool on, auto addr, float wt) {
+      if (on) atomicAdd(acc + addr, __float_as_int(fmaf(wt, rs, kMagic)) - kMagicBits);
+    };
+    if (cone_index32(S.n, S.nz))
+      cone_walk<int>(w, S.n, S.n, S.nz, seg, none);
+    else
+      cone_walk<int64_t>(w, S.n, S.n, S.nz, seg, none);
+  }
+}
+
+// per voxel, over the pixel-pass CTAs: the chunk's 32-bit sums into the
+// 64-bit ones, leaving the 32-bit sums zero for the next chunk
+__global__ void __launch_bounds__(256) cone_bp_fold_kernel(const Launch L) {
   const int scan = L.scans ? find_scan(L.prefix, L.nscans, blockIdx.x) : 0;
   const ScanDev &S = scan_of(L, scan);
   if (!flow_active(S, L.flow)) return;
   const int cta0 = L.scans ? __ldg(L.prefix + scan) : 0;
   const int local_cta = blockIdx.x - cta0;
-  const int64_t item = (int64_t)local_cta * kConeThreads + threadIdx.x;
-  const int sexp = cone_bp_sexp(S);
-  if (item >= S.nbins) return;
-  const int64_t ray = cone_bin_of(S, item);
-  const float r = S.buf[L.in_buf][ray];
-  if (r == 0.f) return;
-  const float rs = r * ldexpf(1.f, sexp);
-  constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
-  constexpr int kMagicBits = 0x4B400000;
-  ConeWalk w = cone_ray(S, ray);
-  if (w.empty) return;
-  unsigned long long *acc = S.bp_acc;
-  auto seg = [&](bool on, auto addr, float wt) {
-    if (on) {
-      const long long term = (long long)(__float_as_int(fmaf(wt, rs, kMagic)) - kMagicBits);
-      atomicAdd(acc + addr, (unsigned long long)term);
+  const int n = S.n, tiles_y = (n + 31) >> 5, tiles = ((n + kPixRows - 1) / kPixRows) * tiles_y;
+  const int z = local_cta / tiles, t = local_cta % tiles;
+  const int y = (t % tiles_y) * 32 + (threadIdx.x & 31);
+#pragma unroll
+  for (int j = 0; j < kPixRows / 8; j++) {
+    const int x = (t / tiles_y) * kPixRows + j * 8 + (threadIdx.x >> 5);
+    if (x < n && y < n && z < S.nz) {
+      const int64_t i = ((int64_t)z * n + x) * n + y;
+      const int part = S.bp_acc32[i];
+      if (part != 0) {
+        S.bp_acc[i] += (unsigned long long)(long long)part;
+        S.bp_acc32[i] = 0;
+      }
     }
-  };
-  auto none = [] {};
-  if (cone_index32(S.n, S.nz))
-    cone_walk<int>(w, S.n, S.n, S.nz, seg, none);
-  else
-    cone_walk<int64_t>(w, S.n, S.n, S.nz, seg, none);
+  }
 }
 
 // per voxel, over the pixel-pass CTAs (kPixRows x 32 tiles of each slice,
-// each thread kPixRows / 8 rows 8 apart)
+// each thread kPixRows / 8 rows 8 apart): the last chunk's sums added to the
+// 64-bit ones, converted, the epilogue run, and both accumulators left zero
 __global__ void __launch_bounds__(256) cone_bp_finish_kernel(const Launch L) {
   const int scan = L.scans ? find_scan(L.prefix, L.nscans, blockIdx.x) : 0;
   const ScanDev &S = scan_of(L, scan);
@@ -336,7 +386,9 @@ __global__ void __launch_bounds__(256) cone_bp_finish_kernel(const Launch L) {
     const int x = (t / tiles_y) * kPixRows + j * 8 + (threadIdx.x >> 5);
     if (x < n && y < n && z < S.nz) {
       const int64_t i = ((int64_t)z * n + x) * n + y;
-      const long long total = (long long)atomicExch(S.bp_acc + i, 0ull);
+      const long long total = (long long)S.bp_acc[i] + S.bp_acc32[i];
+      S.bp_acc[i] = 0ull;
+      S.bp_acc32[i] = 0;
       const float val = (float)((double)total * ldexp(1.0, -sexp));
       bp_epilogue(S, L, z, x, y, val, s0);
     }
@@ -397,6 +449,35 @@ __global__ void cone_trace_one_kernel(const ScanDev S, int64_t ray, int cap, int
 
 int cone_ctas(const ScanDev &S) { return (int)(((int64_t)S.nbins + kConeThreads - 1) / kConeThreads); }
 
+// CTAs of one back-projection chunk (the rays of bp_vchunk views, one per thread)
+int cone_bp_ctas(const ScanDev &S) {
+  const int64_t items = (int64_t)std::min(S.nviews, std::max(1, S.bp_vchunk)) * S.ndets;
+  return (int)((items + kConeThreads - 1) / kConeThreads);
+}
+
+// Views per back-projection chunk.  All rays of a view leave the source point;
+// the detector cell centres lie on a grid of pitch p.  A voxel of edge a whose
+// nearest point is at depth d >= dmin from the source (dmin = SOD minus the
+// volume's radius about the rotation axis) casts a shadow of diameter at most
+// sqrt(3) a (SDD / dmin) (1 + tan_max) on the detector, tan_max bounding the
+// ratio of a point's distance from the central axis to its depth; at most
+// (floor(diameter / p) + 1)^2 cell centres fall in it, so that many rays per
+// view cross the voxel, each once.  Terms are below 2^22, so a 32-bit sum
+// stays exact for 2^9 terms; chunks are sized for half that.
+int cone_bp_views_per_chunk(const at_cone_geometry &g) {
+  const double a = g.voxel_mm;
+  const double R = 0.5 * a * std::sqrt((double)g.nx * g.nx + (double)g.ny * g.ny);
+  const double Z = 0.5 * a * g.nz;
+  const double dmin = (double)g.sod_mm - R;
+  if (!(dmin > 0.0)) return 1;
+  const double tan_max = std::sqrt(R * R + Z * Z) / dmin;
+  const double diam = std::sqrt(3.0) * a * ((double)g.sdd_mm / dmin) * (1.0 + tan_max);
+  const double per_axis = std::floor(diam / (double)g.pitch_mm) + 1.0;
+  const double per_view = per_axis * per_axis;
+  const double v = std::floor(256.0 / per_view);
+  return (int)std::max(1.0, std::min(v, (double)g.nproj));
+}
+
 cudaError_t launch_cone_fp(const Launch &L, int nctas, cudaStream_t st) {
   cone_fp_kernel<<<nctas, kConeThreads, 0, st>>>(L);
   return cudaGetLastError();
@@ -404,11 +485,22 @@ cudaError_t launch_cone_fp(const Launch &L, int nctas, cudaStream_t st) {
 
 // the max |r| pass has run; tracing pass over `L` (ray CTAs), then the
 // finishing pass over `Lpix` (pixel-pass CTAs)
+// (and L.chunks chunks of views, each folded into the 64-bit sums before the
+// next; the last one is added by the finishing pass)
 cudaError_t launch_cone_bp(const Launch &L, int nctas, const Launch &Lpix, int pix_nctas, cudaStream_t st) {
-  cone_bp_kernel<<<nctas, kConeThreads, 0, st>>>(L);
+  const int chunks = std::max(1, L.chunks);
+  for (int c = 0; c < chunks; c++) {
+    Launch Lc = L;
+    Lc.chunk = c;
+    cone_bp_kernel<<<nctas, kConeThreads, 0, st>>>(Lc);
+    if (c + 1 < chunks) cone_bp_fold_kernel<<<pix_nctas, 256, 0, st>>>(Lpix);
+  }
   cone_bp_finish_kernel<<<pix_nctas, 256, 0, st>>>(Lpix);
   return cudaGetLastError();
 }
+
+// launches of one cone back projection (max |r| pass, chunks, folds, finish)
+int cone_bp_launches(int chunks) { return 2 * std::max(1, chunks) + 1; }
 
 int build_cone_plan(Plan &p, cudaStream_t st) {
   const at_cone_geometry &g = p.cone;
@@ -417,6 +509,7 @@ int build_cone_plan(Plan &p, cudaStream_t st) {
   p.nviews = g.nproj;
   p.ndets = g.ndx * g.ndy;
   p.rays = (int64_t)p.nviews * p.ndets;
+  p.cone_bp_views = cone_bp_views_per_chunk(g);
   std::vector<float2> trig(g.nproj);
   cone_trig(g, trig.data());
   AT_CUDA_TRY(cudaMalloc(&p.cone_trig_d, sizeof(float2) * g.nproj));

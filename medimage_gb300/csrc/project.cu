@@ -804,9 +804,11 @@ int fp_group_ctas(const ScanDev &S) {
   return (S.nviews * S.nbpv * 4 + w - 1) / w;
 }
 
+int cone_bp_ctas(const ScanDev &S);
+
 int bp_ctas(const ScanDev &S) {
   if (S.kind == AT_GEOM_GOLDNC) return (kGcN / 8) * (kGcN / 32);
-  if (S.kind == AT_GEOM_CONE) return cone_ctas(S);
+  if (S.kind == AT_GEOM_CONE) return cone_bp_ctas(S);
   return S.ntiles_y * S.ntiles_y * std::max(1, S.bp_split);
 }
 

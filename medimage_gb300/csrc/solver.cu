@@ -26,6 +26,7 @@ int launch_fp_group(const Launch &L, const Launch &Lpix, const Launch &L1, const
 int launch_fp_tr(const Launch &L, const Launch &Lpix, int rpt, int nctas, int pix_nctas, const SlabLaunch *slab,
                  cudaStream_t st);
 int slab_ctas(const ScanDev &S);
+int cone_bp_launches(int chunks);
 size_t slab_smem_bytes(int G, int rows, int wbox);
 int encode_pack_tmap(CUtensorMap *out, const void *pack, int n, int G, int wbox, int rows);
 int launch_bp_group(const Launch &L, const Launch &Lsino, const Launch &Lsmall, int nctas, int sino_nctas,
@@ -68,6 +69,7 @@ void fill_scan_plan(ScanDev &S, const Plan &p) {
   S.sod = p.cone.sod_mm;
   S.sdd = p.cone.sdd_mm;
   S.cone_trig = p.cone_trig_d;
+  S.bp_vchunk = p.cone_bp_views;
   if (p.slab.ok) {
     S.slab_views = p.slab.views;
     S.slab_rays = p.slab.rays;
@@ -139,8 +141,9 @@ void carve_scan(ScanDev &S, const Plan &p, int rpt, char *cur) {
 
 size_t bp_scratch_bytes(const Plan &p) {
   if (p.kind == AT_GEOM_GOLDNC) return 0;
-  return align_up(sizeof(unsigned long long) * (size_t)p.nz * p.n * p.n) + align_up(sizeof(int) * (size_t)p.ntiles) +
-         align_up(sizeof(float) * kBpMaxParts);
+  const size_t npix = (size_t)p.nz * p.n * p.n;
+  return align_up(sizeof(unsigned long long) * npix) + align_up(sizeof(int) * (size_t)p.ntiles) +
+         align_up(sizeof(float) * kBpMaxParts) + (p.kind == AT_GEOM_CONE ? align_up(sizeof(int) * npix) : 0);
 }
 
 void carve_bp_scratch(ScanDev &S, const Plan &p, char *cur) {
@@ -151,6 +154,8 @@ void carve_bp_scratch(ScanDev &S, const Plan &p, char *cur) {
   S.bp_cnt = (int *)cur;
   cur += align_up(sizeof(int) * (size_t)p.ntiles);
   S.bpmax = (float *)cur;
+  cur += align_up(sizeof(float) * kBpMaxParts);
+  if (p.kind == AT_GEOM_CONE) S.bp_acc32 = (int *)cur;
 }
 
 Ctl make_ctl(const at_params &prm) {
@@ -252,6 +257,9 @@ int Batch::set(const ScanDev *scans, int n, int kind_, int rpt_, cudaStream_t st
     AT_CUDA_TRY(cudaMemcpyAsync(tmaps_d, maps.data(), sizeof(CUtensorMap) * n, cudaMemcpyHostToDevice, st));
   }
   scans = sc.data();
+  cone_chunks = 1;
+  for (const auto &S : sc)
+    if (S.kind == AT_GEOM_CONE) cone_chunks = std::max(cone_chunks, (S.nviews + S.bp_vchunk - 1) / std::max(1, S.bp_vchunk));
   std::vector<int> pref(kFamilies * (n + 1), 0);
   auto add = [&](int fam, int s, int ctas) { pref[fam * (n + 1) + s + 1] = pref[fam * (n + 1) + s] + ctas; };
   for (int s = 0; s < n; s++) {
@@ -342,6 +350,7 @@ Launch Batch::base_launch(int family) const {
   L.prefix = prefix_d + family * (nscans + 1);
   L.aux_buf = -1;
   L.group = (family == FAM_PIX || family == FAM_SINO) ? 1 : group;
+  L.chunks = cone_chunks;
   const bool fp = family == FAM_FP || family == FAM_FP1 || family == FAM_FP2;
   if (persistent && (family == FAM_BP || family == FAM_BPS || (fp && !slab))) {
     L.queue = queue_d;
@@ -382,8 +391,8 @@ int Batch::enqueue_bp(const Launch &L, cudaStream_t st) {
   }
   const Launch Lp = retarget(L, FAM_PIX);  // the per-pixel finishing pass of the cone-beam back projector
   AT_CUDA_TRY(launch_bp(L, kind, bp_total, st, &Lp, pix_total));
-  // max |r| pass + back projection (+ per-pixel finish for the cone beam)
-  launches += kind == AT_GEOM_GOLDNC ? 1 : kind == AT_GEOM_CONE ? 3 : 2;
+  // max |r| pass + back projection (cone beam: its chunks, folds and per-pixel finish)
+  launches += kind == AT_GEOM_GOLDNC ? 1 : kind == AT_GEOM_CONE ? cone_bp_launches(cone_chunks) : 2;
   return AT_OK;
 }
 

@@ -37,6 +37,7 @@ struct Batch {
   int *prefix_d = nullptr;  // [kFamilies][cap+1]: CTAs per scan of each family
   int fp_total = 0, pix_total = 0, sino_total = 0, bp_total = 0, fp1_total = 0, fp2_total = 0, bps_total = 0;
   int group = 1;            // largest group of scans sharing a plan (projected together)
+  int cone_chunks = 1;      // cone beam: chunks of views of the batch's largest back projection
   // slab forward projector: used when every plan of the batch has slab tables
   // of one CTA shape; one TMA descriptor per scan (of its pack buffer, in its
   // group's form)

@@ -107,6 +107,11 @@ struct ScanDev {
   float *bpmax;                // [kBpMaxParts]
   unsigned long long *bp_acc;  // [npix]
   int *bp_cnt;                 // [ntiles]
+  // cone beam: 32-bit sums of one chunk of views (folded into bp_acc between
+  // chunks), and the views per chunk, few enough that no voxel's chunk sum
+  // can overflow 32 bits
+  int *bp_acc32;               // [npix]
+  int bp_vchunk;
   int bp_split;                // CTAs per tile (>= 1)
   float4 *pack;                // [max(2*n*n, nbins)] fan/ray plans: a group's projector inputs, interleaved
   // slab forward projector (fan / ray plans with slab tables): the plan's
@@ -140,6 +145,8 @@ struct Launch {
   int in_buf, out_buf, aux_buf;  // buffer ids (meaning depends on the kernel)
   int k;                         // inner iteration this launch belongs to
   int flag;                      // kernel-specific (median this iteration, first pass, ...)
+  int chunk;                     // cone back projection: the chunk of views this launch adds
+  int chunks;                    // cone back projection: chunks of the launch's largest scan (host side)
   int group;                     // projector launches: largest group of scans sharing a plan
   int tr;                        // forward projection: the scans' pack buffers hold transposed inputs
   // persistent launches (projectors of a batch): a grid sized to the resident

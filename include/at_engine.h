@@ -164,6 +164,16 @@ int at_plan_create_rays(int32_t n, double pixel_mm, int32_t nviews, int32_t ndet
  * (helical/rebin/src/tracing.cpp:22-147 applied per ray) has no such knob. */
 int at_plan_set_forward_variant(at_plan *plan, int32_t views, int32_t rays, int32_t rows);
 void at_plan_destroy(at_plan *plan);
+/* Launch form of the projectors of batches (solvers, projection sets, server
+ * groups) made after the call, fan-beam and ray-table plans: 0 = one CTA per
+ * work unit (the default), 1 = persistent, a grid of the resident CTAs pulling
+ * (scan, view, ray block) and (scan, pixel tile) units from a queue, the
+ * costlier scans' units first.  Results are bitwise the same.  On GB300 the
+ * persistent form measured 8-9 % slower (C2, 16 slices; C3): a CTA's finished
+ * warps wait at each unit's end while the hardware scheduler would start a new
+ * CTA beside them.  The reference has no batched form (its only GPU code,
+ * industry3d/cuda/main.cu:530-537, relaunches one kernel per iteration). */
+int at_set_batch_launch_mode(int32_t persistent);
 int at_plan_get_stats(const at_plan *plan, at_plan_stats *out);
 /* Traversal of one ray as the device plan stores it: pixel indices and FP32
  * weights in visiting order.  For AT_GEOM_GOLDNC, (view, det) address the

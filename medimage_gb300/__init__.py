@@ -25,6 +25,7 @@ from .engine import (  # noqa: F401
     lib,
     quality,
     reconstruct,
+    set_batch_launch_mode,
 )
 from . import configs, io, phantom  # noqa: F401
 
@@ -47,4 +48,5 @@ __all__ = [
     "phantom",
     "quality",
     "reconstruct",
+    "set_batch_launch_mode",
 ]

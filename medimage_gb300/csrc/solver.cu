@@ -9,6 +9,7 @@
 // batch in one allocation and captures its outer iteration once as a CUDA
 // graph; the server (server.cu) rebuilds its batch as requests come and go.
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <vector>
 
@@ -173,12 +174,11 @@ Ctl make_ctl(const at_params &prm) {
 }
 
 // ---------------------------------------------------------------- Batch
-// Projector launches of fan-beam / ray-table batches run persistent: a grid of
-// the resident CTAs pulling work units from a queue (set to 0 at build time to
-// launch one CTA per unit instead; results are the same).
-#ifndef MEDIMG_PERSISTENT_BATCHES
-#define MEDIMG_PERSISTENT_BATCHES 1
-#endif
+// Whether batches made from now on run their fan-beam / ray-table projector
+// launches persistent (a grid of the resident CTAs pulling work units from a
+// queue) or one CTA per unit (the default: measured faster on GB300, see
+// at_set_batch_launch_mode).  Results are bitwise the same either way.
+std::atomic<int> g_persistent_batches{0};
 
 Batch::~Batch() {
   cudaFree(scans_d);
@@ -294,7 +294,7 @@ int Batch::set(const ScanDev *scans, int n, int kind_, int rpt_, cudaStream_t st
   // work orders of the persistent projector launches: per family, the units
   // of each scan in their natural order, scans by decreasing work per unit
   // (segments ~ views x detectors x n), so the cheapest units come last
-  persistent = MEDIMG_PERSISTENT_BATCHES && (kind == AT_GEOM_FAN || kind == AT_GEOM_RAYS);
+  persistent = g_persistent_batches.load() != 0 && (kind == AT_GEOM_FAN || kind == AT_GEOM_RAYS);
   if (persistent) {
     std::vector<int> order;
     const int fams[5] = {FAM_FP, FAM_FP1, FAM_FP2, FAM_BP, FAM_BPS};
@@ -684,3 +684,10 @@ int Solver::run(cudaStream_t st) {
 }
 
 }  // namespace medimg
+
+extern "C" __attribute__((visibility("default"))) int at_set_batch_launch_mode(int32_t persistent) {
+  if (persistent != 0 && persistent != 1)
+    return medimg::set_error(AT_EINVAL, "at_set_batch_launch_mode: 0 (one CTA per unit) or 1 (persistent)");
+  medimg::g_persistent_batches.store(persistent);
+  return AT_OK;
+}

@@ -123,6 +123,7 @@ SIGNATURES = {
     "at_plan_create_fan_ex": ([C.POINTER(_FanGeom), C.c_int32, C.POINTER(C.c_void_p)], C.c_int),
     "at_plan_create_goldnc": ([C.POINTER(C.c_void_p)], C.c_int),
     "at_plan_set_forward_variant": ([C.c_void_p, C.c_int32, C.c_int32, C.c_int32], C.c_int),
+    "at_set_batch_launch_mode": ([C.c_int32], C.c_int),
     "at_rowaction_create": ([C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)], C.c_int),
     "at_rowaction_destroy": ([C.c_void_p], None),
     "at_rowaction_segments": ([C.c_void_p, C.POINTER(C.c_int64)], C.c_int),
@@ -637,6 +638,13 @@ class Solver:
         n = C.c_int32()
         _check("at_solver_launches_per_outer", lib().at_solver_launches_per_outer(self._h, C.byref(n)))
         return n.value
+
+
+def set_batch_launch_mode(persistent: bool) -> None:
+    """Launch form of batched projections made from now on: persistent
+    (resident CTAs pulling work units from a queue) or one CTA per unit (the
+    default, measured faster); results are bitwise the same."""
+    _check("at_set_batch_launch_mode", lib().at_set_batch_launch_mode(1 if persistent else 0))
 
 
 def reconstruct(plan: Plan, params: Params, sino: np.ndarray):

@@ -149,11 +149,14 @@ __device__ __forceinline__ ConeWalk cone_start(int nx, int ny, int nz, float sx,
 // the clipped segment, so the walk ends within nx + ny + nz + 3 steps; the
 // block bound is only a guard.  Idx is the voxel index type: 32-bit when
 // every index the walk can form fits (cone_index32).
+// xst / yst: the index strides of x and y (ny and 1 in the volume's layout;
+// 1 and nx for an x-contiguous copy), z slices of nx*ny either way.
 template <typename Idx, typename F, typename B>
-__device__ __forceinline__ void cone_walk(ConeWalk &w, int nx, int ny, int nz, F &&f, B &&end_block) {
+__device__ __forceinline__ void cone_walk_strided(ConeWalk &w, int nx, int ny, int nz, Idx xst, Idx yst, F &&f,
+                                                  B &&end_block) {
   const Idx nxy = (Idx)nx * ny;
-  const Idx sxs = (Idx)w.sx * ny, sys = (Idx)w.sy, szs = (Idx)w.sz * nxy;
-  Idx addr = (Idx)w.vz * nxy + (Idx)w.vx * ny + (Idx)w.vy;
+  const Idx sxs = (Idx)w.sx * xst, sys = (Idx)w.sy * yst, szs = (Idx)w.sz * nxy;
+  Idx addr = (Idx)w.vz * nxy + (Idx)w.vx * xst + (Idx)w.vy * yst;
   const int guard = (nx + ny + nz + 16) / 32 + 2;
   for (int blk = 0; blk < guard; blk++) {
     int j = 0;
@@ -183,6 +186,11 @@ __device__ __forceinline__ void cone_walk(ConeWalk &w, int nx, int ny, int nz, F
     end_block();
     if (j < 32) break;
   }
+}
+
+template <typename Idx, typename F, typename B>
+__device__ __forceinline__ void cone_walk(ConeWalk &w, int nx, int ny, int nz, F &&f, B &&end_block) {
+  cone_walk_strided<Idx>(w, nx, ny, nz, (Idx)ny, (Idx)1, f, end_block);
 }
 
 // 32-bit voxel indices hold every index a walk can form (each coordinate one
@@ -321,7 +329,6 @@ __global__ void __launch_bounds__(kConeThreads) cone_bp_kernel(const Launch L) {
   const int64_t nitems = (int64_t)nv * S.ndets;
   constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
   constexpr int kMagicBits = 0x4B400000;
-  int *acc = S.bp_acc32;
   auto none = [] {};
   for (int64_t item = (int64_t)local_cta * kConeThreads + threadIdx.x; item < nitems;
        item += (int64_t)ncta * kConeThreads) {
@@ -331,13 +338,60 @@ __global__ void __launch_bounds__(kConeThreads) cone_bp_kernel(const Launch L) {
     const float rs = r * scale;
     ConeWalk w = cone_ray(S, ray);
     if (w.empty) continue;
+    // a warp's rays are neighbouring detector columns of one view; they lie
+    // side by side along the view's column direction (cos, sin) in (x, y).
+    // Where that is closer to x, they add into the x-contiguous accumulator,
+    // so the lanes of one atomic instruction share sectors
+    const float2 cs = __ldg(S.cone_trig + (int)(ray / S.ndets));
+    const bool xfast = fabsf(cs.x) > fabsf(cs.y);
+    int *acc = xfast ? S.bp_acc32x : S.bp_acc32;
     auto seg = [&](bool on, auto addr, float wt) {
       if (on) atomicAdd(acc + addr, __float_as_int(fmaf(wt, rs, kMagic)) - kMagicBits);
     };
-    if (cone_index32(S.n, S.nz))
-      cone_walk<int>(w, S.n, S.n, S.nz, seg, none);
-    else
-      cone_walk<int64_t>(w, S.n, S.n, S.nz, seg, none);
+    if (cone_index32(S.n, S.nz)) {
+      if (xfast) cone_walk_strided<int>(w, S.n, S.n, S.nz, 1, S.n, seg, none);
+      else cone_walk<int>(w, S.n, S.n, S.nz, seg, none);
+    } else {
+      if (xfast) cone_walk_strided<int64_t>(w, S.n, S.n, S.nz, (int64_t)1, (int64_t)S.n, seg, none);
+      else cone_walk<int64_t>(w, S.n, S.n, S.nz, seg, none);
+    }
+  }
+}
+
+// The chunk sums of one kPixRows x 32 tile of slice z: the volume-layout
+// accumulator's at (x, y) plus the x-contiguous one's, read through a
+// shared-memory transpose so both reads are coalesced; both left zero.
+__device__ __forceinline__ void cone_chunk_sums(const ScanDev &S, int z, int bx, int by, int (&out)[kPixRows / 8]) {
+  __shared__ int tx[32][kPixRows + 1];
+  const int n = S.n, lane = threadIdx.x & 31, wrow = threadIdx.x >> 5;
+  // x-contiguous copy: row y of slice z holds x = 0..n-1; lanes along x
+#pragma unroll
+  for (int j = 0; j < 32 / 8; j++) {
+    const int yy = by + j * 8 + wrow;
+    for (int xo = lane; xo < kPixRows; xo += 32) {
+      const int xx = bx + xo;
+      int v = 0;
+      if (xx < n && yy < n && z < S.nz) {
+        const int64_t i = ((int64_t)z * n + yy) * n + xx;
+        v = S.bp_acc32x[i];
+        if (v != 0) S.bp_acc32x[i] = 0;
+      }
+      tx[yy - by][xo] = v;
+    }
+  }
+  __syncthreads();
+  const int y = by + lane;
+#pragma unroll
+  for (int j = 0; j < kPixRows / 8; j++) {
+    const int x = bx + j * 8 + wrow;
+    int v = tx[lane][j * 8 + wrow];
+    if (x < n && y < n && z < S.nz) {
+      const int64_t i = ((int64_t)z * n + x) * n + y;
+      const int a = S.bp_acc32[i];
+      if (a != 0) S.bp_acc32[i] = 0;
+      v += a;  // |v| < 2^31: each accumulator's chunk sum is below 2^30
+    }
+    out[j] = v;
   }
 }
 
@@ -352,16 +406,14 @@ __global__ void __launch_bounds__(256) cone_bp_fold_kernel(const Launch L) {
   const int n = S.n, tiles_y = (n + 31) >> 5, tiles = ((n + kPixRows - 1) / kPixRows) * tiles_y;
   const int z = local_cta / tiles, t = local_cta % tiles;
   const int y = (t % tiles_y) * 32 + (threadIdx.x & 31);
+  int part[kPixRows / 8];
+  cone_chunk_sums(S, z, (t / tiles_y) * kPixRows, (t % tiles_y) * 32, part);
 #pragma unroll
   for (int j = 0; j < kPixRows / 8; j++) {
     const int x = (t / tiles_y) * kPixRows + j * 8 + (threadIdx.x >> 5);
-    if (x < n && y < n && z < S.nz) {
+    if (x < n && y < n && z < S.nz && part[j] != 0) {
       const int64_t i = ((int64_t)z * n + x) * n + y;
-      const int part = S.bp_acc32[i];
-      if (part != 0) {
-        S.bp_acc[i] += (unsigned long long)(long long)part;
-        S.bp_acc32[i] = 0;
-      }
+      S.bp_acc[i] += (unsigned long long)(long long)part[j];
     }
   }
 }
@@ -380,15 +432,16 @@ __global__ void __launch_bounds__(256) cone_bp_finish_kernel(const Launch L) {
   const int z = local_cta / tiles, t = local_cta % tiles;
   const int y = (t % tiles_y) * 32 + (threadIdx.x & 31);
   const int sexp = cone_bp_sexp(S);
+  int part[kPixRows / 8];
+  cone_chunk_sums(S, z, (t / tiles_y) * kPixRows, (t % tiles_y) * 32, part);
   FF s0 = ff_zero();
 #pragma unroll
   for (int j = 0; j < kPixRows / 8; j++) {
     const int x = (t / tiles_y) * kPixRows + j * 8 + (threadIdx.x >> 5);
     if (x < n && y < n && z < S.nz) {
       const int64_t i = ((int64_t)z * n + x) * n + y;
-      const long long total = (long long)S.bp_acc[i] + S.bp_acc32[i];
+      const long long total = (long long)S.bp_acc[i] + part[j];
       S.bp_acc[i] = 0ull;
-      S.bp_acc32[i] = 0;
       const float val = (float)((double)total * ldexp(1.0, -sexp));
       bp_epilogue(S, L, z, x, y, val, s0);
     }

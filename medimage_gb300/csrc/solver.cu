@@ -144,7 +144,7 @@ size_t bp_scratch_bytes(const Plan &p) {
   if (p.kind == AT_GEOM_GOLDNC) return 0;
   const size_t npix = (size_t)p.nz * p.n * p.n;
   return align_up(sizeof(unsigned long long) * npix) + align_up(sizeof(int) * (size_t)p.ntiles) +
-         align_up(sizeof(float) * kBpMaxParts) + (p.kind == AT_GEOM_CONE ? align_up(sizeof(int) * npix) : 0);
+         align_up(sizeof(float) * kBpMaxParts) + (p.kind == AT_GEOM_CONE ? 2 * align_up(sizeof(int) * npix) : 0);
 }
 
 void carve_bp_scratch(ScanDev &S, const Plan &p, char *cur) {
@@ -156,7 +156,11 @@ void carve_bp_scratch(ScanDev &S, const Plan &p, char *cur) {
   cur += align_up(sizeof(int) * (size_t)p.ntiles);
   S.bpmax = (float *)cur;
   cur += align_up(sizeof(float) * kBpMaxParts);
-  if (p.kind == AT_GEOM_CONE) S.bp_acc32 = (int *)cur;
+  if (p.kind == AT_GEOM_CONE) {
+    const size_t npix = (size_t)p.nz * p.n * p.n;
+    S.bp_acc32 = (int *)cur;
+    S.bp_acc32x = (int *)(cur + align_up(sizeof(int) * npix));
+  }
 }
 
 Ctl make_ctl(const at_params &prm) {

@@ -110,7 +110,8 @@ struct ScanDev {
   // cone beam: 32-bit sums of one chunk of views (folded into bp_acc between
   // chunks), and the views per chunk, few enough that no voxel's chunk sum
   // can overflow 32 bits
-  int *bp_acc32;               // [npix]
+  int *bp_acc32;               // [npix] volume layout (y contiguous)
+  int *bp_acc32x;              // [npix] x contiguous: (z*n + y)*n + x
   int bp_vchunk;
   int bp_split;                // CTAs per tile (>= 1)
   float4 *pack;                // [max(2*n*n, nbins)] fan/ray plans: a group's projector inputs, interleaved

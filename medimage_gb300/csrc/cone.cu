@@ -306,6 +306,12 @@ __device__ __forceinline__ int cone_bp_sexp(const ScanDev &S) {
   return s_sexp;
 }
 
+// v added to *p as a reduction (PTX red: no value comes back, so the walk
+// never waits on it)
+__device__ __forceinline__ void red_add(int *p, int v) {
+  asm volatile("red.relaxed.gpu.global.add.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
 // One chunk of views (L.chunk; S.bp_vchunk views each), rays in band order,
 // a grid-stride loop over the chunk's rays.  Each term w*r is rounded to an
 // integer below 2^22 (one FFMA, magic-number rounding) and added with a 32-bit
@@ -346,7 +352,7 @@ __global__ void __launch_bounds__(kConeThreads) cone_bp_kernel(const Launch L) {
     const bool xfast = fabsf(cs.x) > fabsf(cs.y);
     int *acc = xfast ? S.bp_acc32x : S.bp_acc32;
     auto seg = [&](bool on, auto addr, float wt) {
-      if (on) atomicAdd(acc + addr, __float_as_int(fmaf(wt, rs, kMagic)) - kMagicBits);
+      if (on) red_add(acc + addr, __float_as_int(fmaf(wt, rs, kMagic)) - kMagicBits);
     };
     if (cone_index32(S.n, S.nz)) {
       if (xfast) cone_walk_strided<int>(w, S.n, S.n, S.nz, 1, S.n, seg, none);

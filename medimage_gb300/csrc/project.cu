@@ -404,6 +404,12 @@ __global__ void __launch_bounds__(256) sino_absmax_kernel(const Launch L) {
   }
 }
 
+// v added to the shared-memory word *p as a reduction (PTX red: no value
+// comes back, so the walk never waits on it)
+__device__ __forceinline__ void red_shared_add(int *p, int v) {
+  asm volatile("red.shared.add.s32 [%0], %1;" ::"r"((unsigned)__cvta_generic_to_shared(p)), "r"(v) : "memory");
+}
+
 template <int G, int C>
 __device__ __forceinline__ void fan_bp_body(const Launch &L, const int unit) {
   constexpr int kStride = bp_copy_stride<C>();  // one copy
@@ -536,7 +542,7 @@ __device__ __forceinline__ void fan_bp_body(const Launch &L, const int unit) {
           prev = cur;
 #pragma unroll
           for (int m = 0; m < G; m++)
-            if (use[m]) atomicAdd(&my_acc[m * kMemStride + sidx], __float_as_int(fmaf(wt, rs[m], kMagic)) - kMagicBits);
+            if (use[m]) red_shared_add(&my_acc[m * kMemStride + sidx], __float_as_int(fmaf(wt, rs[m], kMagic)) - kMagicBits);
           sidx += bx ? dsx : dsy;
           cxf += bx ? 1.f : 0.f;
           cyf += bx ? 0.f : 1.f;
@@ -552,7 +558,7 @@ __device__ __forceinline__ void fan_bp_body(const Launch &L, const int unit) {
           if (t < nk)
 #pragma unroll
             for (int m = 0; m < G; m++)
-              if (use[m]) atomicAdd(&my_acc[m * kMemStride + sidx], __float_as_int(fmaf(wt, rs[m], kMagic)) - kMagicBits);
+              if (use[m]) red_shared_add(&my_acc[m * kMemStride + sidx], __float_as_int(fmaf(wt, rs[m], kMagic)) - kMagicBits);
           sidx += bx ? dsx : dsy;
           cxf += bx ? 1.f : 0.f;
           cyf += bx ? 0.f : 1.f;

@@ -120,6 +120,11 @@ typedef struct at_plan_stats {
      * detectors), rows per slab, staged columns per slab, and the CTAs that
      * gather through L1 because a ray leaves the grid; all 0 otherwise */
     int32_t slab_views, slab_rays, slab_rows, slab_wbox, slab_fallback_ctas;
+    /* back projection from the pixel table (at_plan_set_back_variant): the
+     * launches that use it (bit0 single scans, bit1 groups of scans sharing
+     * the plan), the table's bytes in HBM and its weights; 0 without one */
+    int32_t bp_table_use;
+    int64_t bp_table_bytes, bp_table_weights;
 } at_plan_stats;
 
 const char *at_last_error(void);
@@ -163,6 +168,21 @@ int at_plan_create_rays(int32_t n, double pixel_mm, int32_t nviews, int32_t ndet
  * The forward projector of the reference
  * (helical/rebin/src/tracing.cpp:22-147 applied per ray) has no such knob. */
 int at_plan_set_forward_variant(at_plan *plan, int32_t views, int32_t rays, int32_t rows);
+/* Selects the back projector of a fan-beam or ray-table plan for launches of
+ * single scans (use bit0) and of groups of scans that share the plan (bit1):
+ * a set bit gathers each pixel's terms from the plan's pixel table (the
+ * traversal stored by pixel and view, with each segment's FP32 weight; built
+ * on the first call that asks for it, about 4 bytes per segment plus 4 per
+ * pixel and view), a clear bit walks the (ray, 16x16 tile) runs.  Results
+ * are bitwise the same either way: both add the same fixed-point terms.
+ * AT_EINVAL for a mask outside 0..3 or a plan the table's fields cannot hold
+ * (more than 32767 detectors, or 63 rays of one view through one pixel).
+ * Solvers, projection sets and servers made before the call keep the variant
+ * they were made with; the table stays until the plan is destroyed.  Not
+ * thread-safe against concurrent calls on the same plan.  The reference's
+ * back projector (helical/rebin/src/tracing.cpp:22-147, transposed per ray)
+ * has no such knob. */
+int at_plan_set_back_variant(at_plan *plan, int32_t use);
 void at_plan_destroy(at_plan *plan);
 /* Launch form of the projectors of batches (solvers, projection sets, server
  * groups) made after the call, fan-beam and ray-table plans: 0 = one CTA per

@@ -30,6 +30,7 @@ namespace medimg {
 constexpr int kRayBlock = 128;  // rays per decision-bit block (one view)
 constexpr int kBpTile = 16;     // back-projection tile edge (pixels)
 constexpr int kBpViewBlock = 64;  // views whose contributions share one 32-bit accumulator
+constexpr int kPtChunk = 16;      // views per chunk of a pixel-table stream (prefetched as one)
 
 // Per-ray header.  Boundary parameters are relative to the ray's entry
 // lambda_min (mm): the k-th x-plane crossing is at fmaf(k, lenx, ax), the k-th
@@ -113,6 +114,22 @@ struct Plan {
   int ntiles_y = 0, ntiles = 0, nvb = 0;
   int bp_term_bits = 24;           // fixed-point bits of one back-projection term
   int64_t nruns = 0;
+  // back projection by pixel: the traversal's transpose, stored.  A stream is
+  // one warp's 4x8 pixel block of a 16x16 tile (stream = tile * 8 + warp;
+  // warp = (x%16)/4 * 2 + (y%16)/8, lane = (x%4) * 8 + y%8).  Per (stream,
+  // view, lane) one word d0 | n << 15 | pre << 21: the rays of that view
+  // crossing the pixel are bins view*ndets + d0 .. + n-1, and their weights
+  // (0 for a ray between them that misses the pixel) sit at pt_w[view's
+  // first weight in the stream + pre + k], pre = the lane's position among
+  // the warp's weights of that view.  pt_woff[stream * (nch + 1) + c]: the
+  // first weight of chunk c (views c*kPtChunk ..) in the stream, nch chunks.  Weights are the forward
+  // walk's FP32 segment lengths bit for bit, so each fixed-point term, and
+  // each pixel's integer sum, equals the tile-run back projector's.
+  uint32_t *pt_meta_d = nullptr;
+  float *pt_w_d = nullptr;
+  int64_t *pt_woff_d = nullptr;
+  int64_t pt_entries = 0, pt_bytes = 0;
+  int bp_table = 0;  // launches that back-project from the table: bit0 single scans, bit1 groups
   // goldnc
   GcSeg *gc_seg_d = nullptr;
   int32_t *gc_pair_off_d = nullptr;  // [17280+1]
@@ -163,6 +180,12 @@ int autotune_fan(Plan &p, cudaStream_t st);
 int build_slab_tables(Plan &p, int views, int rays, int rows, cudaStream_t st);
 void free_slab_tables(SlabPlan &s);
 void retire_slab_tables(Plan &p);  // moves p.slab to p.retired_slabs
+// pixel table for the back projector (ptable.cu): AT_OK with p.pt_meta_d null
+// when the plan's shape does not fit the table's fields (more than 32767
+// detectors, 63 rays of one view through a pixel, 2047 weights of one warp's
+// pixels in one view) or the table would exceed max_bytes
+int build_pixel_table(Plan &p, int64_t max_bytes, cudaStream_t st);
+void free_pixel_table(Plan &p);
 
 }  // namespace medimg
 

@@ -1,6 +1,7 @@
 // capi.cu -- the C-ABI of include/at_engine.h and the GoldenC drop-in symbols
 // of include/goldnc.h.
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <memory>
@@ -85,6 +86,7 @@ int project(const Plan &p, bool forward, const float *in, float *out, cudaStream
       carve_bp_scratch(L.single, p, (char *)scratch);
       L.single.bp_split = bp_split_for(p.ntiles, p.nvb);
     }
+    L.bp_table = (L.single.pt_use & 1) ? 1 : 0;
     if (p.kind == AT_GEOM_CONE) L.chunks = (p.nviews + p.cone_bp_views - 1) / std::max(1, p.cone_bp_views);
     e = launch_bp(L, p.kind, bp_ctas(L.single), st, &L, pix_ctas(L.single));
     if (scratch) cudaFreeAsync(scratch, st);
@@ -242,6 +244,25 @@ AT_API int at_plan_set_forward_variant(at_plan *plan, int32_t views, int32_t ray
   return AT_OK;
 }
 
+AT_API int at_plan_set_back_variant(at_plan *plan, int32_t use) {
+  AT_CHECK_ARG(plan, "at_plan_set_back_variant: null plan");
+  Plan &p = plan->p;
+  AT_CHECK_ARG(p.kind == AT_GEOM_FAN || p.kind == AT_GEOM_RAYS,
+               "at_plan_set_back_variant: fan-beam and ray-table plans only");
+  AT_CHECK_ARG(use >= 0 && use <= 3, "at_plan_set_back_variant: use is a mask of 1 (single scans) and 2 (groups)");
+  if (use && !p.pt_meta_d) {
+    cudaStream_t st;
+    AT_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    const int rc = build_pixel_table(p, INT64_MAX, st);
+    cudaStreamSynchronize(st);
+    cudaStreamDestroy(st);
+    if (rc) return rc;
+    if (!p.pt_meta_d) return set_error(AT_EINVAL, "at_plan_set_back_variant: the pixel table does not fit this plan");
+  }
+  p.bp_table = use;
+  return AT_OK;
+}
+
 AT_API int at_plan_get_stats(const at_plan *plan, at_plan_stats *out) {
   AT_CHECK_ARG(plan && out, "at_plan_get_stats: null argument");
   const Plan &p = plan->p;
@@ -262,6 +283,9 @@ AT_API int at_plan_get_stats(const at_plan *plan, at_plan_stats *out) {
   out->slab_rows = p.slab.ok ? p.slab.rows : 0;
   out->slab_wbox = p.slab.ok ? p.slab.wbox : 0;
   out->slab_fallback_ctas = p.slab.ok ? p.slab.fallback : 0;
+  out->bp_table_use = p.pt_meta_d ? p.bp_table : 0;
+  out->bp_table_bytes = p.pt_bytes;
+  out->bp_table_weights = p.pt_entries;
   return AT_OK;
 }
 

@@ -410,7 +410,146 @@ __device__ __forceinline__ void red_shared_add(int *p, int v) {
   asm volatile("red.shared.add.s32 [%0], %1;" ::"r"((unsigned)__cvta_generic_to_shared(p)), "r"(v) : "memory");
 }
 
-template <int G, int C>
+// The residuals of bin for the G members: one float, or the group's
+// interleaved float2 / float4.
+template <int G>
+__device__ __forceinline__ void bp_load_r(const float *__restrict__ sino, const float4 *__restrict__ spack,
+                                          unsigned bin, float (&r)[G]) {
+  if constexpr (G == 1) {
+    r[0] = __ldg(sino + bin);
+  } else if constexpr (G == 2) {
+    const float2 v = __ldg(reinterpret_cast<const float2 *>(spack) + bin);
+    r[0] = v.x;
+    r[1] = v.y;
+  } else {
+    static_assert(G == 4, "members are read as one float, float2 or float4");
+    const float4 v = __ldg(spack + bin);
+    r[0] = v.x;
+    r[1] = v.y;
+    r[2] = v.z;
+    r[3] = v.w;
+  }
+}
+
+// w*r*scale + 1.5*2^23 rounds w*r*scale to an integer in the float's low
+// mantissa bits (|w*r*scale| < 2^22), so one FFMA does the scaling and the
+// round-to-nearest conversion
+constexpr float kBpMagic = 12582912.0f;  // 1.5 * 2^23
+constexpr int kBpMagicBits = 0x4B400000;
+
+// bytes at p (16-byte aligned, a multiple of 16) fetched into L2 ahead of use
+__device__ __forceinline__ void prefetch_l2(const void *p, unsigned bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
+// Back projection from the plan's pixel table: thread (warp, lane) owns pixel
+// ((warp/2)*4 + lane/8, (warp%2)*8 + lane%8) of the tile and gathers, view by
+// view, the terms of the rays that cross it, in the same fixed point as the
+// tile-run walk (32-bit sums per view block, folded into 64 bits).  Each warp
+// reads its own stream (the table's words and weights of its 32 pixels, view
+// after view); one lane asks L2 for the stream's chunks of kPtChunk views two
+// chunks ahead, so the loads of a view wait on L2, not on HBM.  Returns the
+// sums in the tile-run mapping (thread x*16 + y), through shared memory.
+template <int G>
+__device__ __forceinline__ void bp_table_sums(const ScanDev &S, const float *__restrict__ sino,
+                                              const float4 *__restrict__ spack, int tile, int vb0, int vb1,
+                                              const float (&scale)[G], const bool (&use)[G], long long (&total)[G],
+                                              long long *xch) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const size_t stream = (size_t)tile * 8 + warp;
+  const int nch = (S.nviews + kPtChunk - 1) / kPtChunk;
+  const uint32_t *__restrict__ meta0 = S.pt_meta + stream * (size_t)S.nviews * 32;
+  const uint32_t *__restrict__ meta = meta0 + lane;
+  const int64_t *__restrict__ woff = S.pt_woff + stream * (size_t)(nch + 1);
+  const int ch_end = (min(S.nviews, vb1 * kBpViewBlock) + kPtChunk - 1) / kPtChunk;
+  auto prefetch_chunk = [&](int c) {
+    if (lane == 0 && c < ch_end) {
+      const int cv0 = c * kPtChunk, cv1 = min(S.nviews, cv0 + kPtChunk);
+      prefetch_l2(meta0 + (size_t)cv0 * 32, (unsigned)(cv1 - cv0) * 128u);
+      const int64_t a = __ldg(woff + c) & ~3ll, b = (__ldg(woff + c + 1) + 3) & ~3ll;
+      if (b > a) prefetch_l2(S.pt_w + a, (unsigned)(b - a) * 4u);
+    }
+  };
+  static_assert(kBpViewBlock % kPtChunk == 0, "view blocks are whole chunks");
+  prefetch_chunk(vb0 * (kBpViewBlock / kPtChunk));
+  prefetch_chunk(vb0 * (kBpViewBlock / kPtChunk) + 1);
+  // Views go V at a time: a lane's rays of those views are numbered as slots
+  // 0..E-1 (view j's rays from p[j]), and the loads of U slots issue together,
+  // so one round trip to memory serves several views.
+  constexpr int V = G == 4 ? 2 : 4;
+  constexpr int U = G == 4 ? 4 : 8;
+  static_assert(kPtChunk % V == 0 && kBpViewBlock % V == 0, "view groups stay inside a chunk");
+  for (int vb = vb0; vb < vb1; vb++) {
+    const int v0 = vb * kBpViewBlock, v1 = min(S.nviews, v0 + kBpViewBlock);
+    const float *__restrict__ wblk = S.pt_w + __ldg(woff + vb * (kBpViewBlock / kPtChunk));
+    int wrun = 0;  // the view's first weight, from wblk
+    int acc[G];
+#pragma unroll
+    for (int m = 0; m < G; m++) acc[m] = 0;
+    uint32_t mn[V];
+#pragma unroll
+    for (int j = 0; j < V; j++) mn[j] = (v0 + j < v1) ? __ldg(meta + (size_t)(v0 + j) * 32) : 0u;
+    for (int v = v0; v < v1; v += V) {
+      if (v % kPtChunk == 0) prefetch_chunk(v / kPtChunk + 2);
+      uint32_t mc[V];
+#pragma unroll
+      for (int j = 0; j < V; j++) {
+        mc[j] = mn[j];
+        mn[j] = (v + V + j < v1) ? __ldg(meta + (size_t)(v + V + j) * 32) : 0u;
+      }
+      // slot s of view j: weight wblk[wo[j] + s], bin bo[j] + s
+      int p[V + 1], wo[V], bo[V];
+      p[0] = 0;
+#pragma unroll
+      for (int j = 0; j < V; j++) {
+        const int d0 = (int)(mc[j] & 0x7fffu), n = (int)((mc[j] >> 15) & 63u), pre = (int)(mc[j] >> 21);
+        wo[j] = wrun + pre - p[j];
+        bo[j] = (v + j) * S.ndets + d0 - p[j];
+        p[j + 1] = p[j] + n;
+        wrun += __shfl_sync(0xffffffffu, pre + n, 31);
+      }
+      const int E = p[V];
+      const int emax = (int)__reduce_max_sync(0xffffffffu, (unsigned)E);
+      for (int s0 = 0; s0 < emax; s0 += U) {
+        float wt[U], r[U][G];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+          const int sl = s0 + u;
+          int a = wo[0], b = bo[0];
+#pragma unroll
+          for (int j = 1; j < V; j++)
+            if (sl >= p[j]) {
+              a = wo[j];
+              b = bo[j];
+            }
+          wt[u] = 0.f;
+#pragma unroll
+          for (int m = 0; m < G; m++) r[u][m] = 0.f;
+          if (sl < E) {
+            wt[u] = __ldg(wblk + a + sl);
+            bp_load_r<G>(sino, spack, (unsigned)(b + sl), r[u]);
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++)
+          if (s0 + u < E)
+#pragma unroll
+            for (int m = 0; m < G; m++)
+              if (use[m]) acc[m] += __float_as_int(fmaf(wt[u], r[u][m] * scale[m], kBpMagic)) - kBpMagicBits;
+      }
+    }
+#pragma unroll
+    for (int m = 0; m < G; m++) total[m] += acc[m];
+  }
+  const int own = (((warp >> 1) << 2) + (lane >> 3)) * kBpTile + ((warp & 1) << 3) + (lane & 7);
+#pragma unroll
+  for (int m = 0; m < G; m++) xch[m * 256 + own] = total[m];
+  __syncthreads();
+#pragma unroll
+  for (int m = 0; m < G; m++) total[m] = xch[m * 256 + threadIdx.x];
+}
+
+template <int G, int C, int kMode>
 __device__ __forceinline__ void fan_bp_body(const Launch &L, const int unit) {
   constexpr int kStride = bp_copy_stride<C>();  // one copy
   constexpr int kMemStride = C * kStride;       // one member
@@ -436,10 +575,15 @@ __device__ __forceinline__ void fan_bp_body(const Launch &L, const int unit) {
   const int vb0 = split * S.nvb / S.bp_split, vb1 = (split + 1) * S.nvb / S.bp_split;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const bool real = split < S.bp_split;
-  __shared__ int acc[G * kMemStride];
+  // gather from the pixel table instead of walking tile runs (kMode: the
+  // launch's Launch::bp_table)
+  const bool table = kMode == 1 || (kMode == 2 && (S.pt_use & (nm > 1 ? 2 : 1)) != 0);
+  static_assert(kMemStride >= 512, "the accumulators double as the table path's 64-bit exchange");
+  __shared__ __align__(16) int acc[kMode == 1 ? G * 512 : G * kMemStride];
   __shared__ float wmax[G][8];
   __shared__ int last_split;
-  for (int i = threadIdx.x; i < G * kMemStride; i += blockDim.x) acc[i] = 0;
+  if (!table)
+    for (int i = threadIdx.x; i < G * kMemStride; i += blockDim.x) acc[i] = 0;
   int *const my_acc = acc + (lane % C) * kStride;
   // one scan: its sinogram; a group: the members' sinograms interleaved, one
   // float4 per bin (the lead's pack buffer)
@@ -477,12 +621,12 @@ __device__ __forceinline__ void fan_bp_body(const Launch &L, const int unit) {
   long long total[G];  // exact sums over view blocks
 #pragma unroll
   for (int m = 0; m < G; m++) total[m] = 0;
-  // w*r*scale + 1.5*2^23 rounds w*r*scale to an integer in the float's low
-  // mantissa bits (|w*r*scale| < 2^22), so one FFMA does the scaling and the
-  // round-to-nearest conversion
-  constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
-  constexpr int kMagicBits = 0x4B400000;
-  if (any_use) {
+  constexpr float kMagic = kBpMagic;
+  constexpr int kMagicBits = kBpMagicBits;
+  if (table) {
+    if (any_use)
+      bp_table_sums<G>(S, sino, spack, tile, vb0, vb1, scale, use, total, reinterpret_cast<long long *>(acc));
+  } else if (any_use) {
     for (int vb = vb0; vb < vb1; vb++) {
       const int b0 = __ldg(toff + vb), b1 = __ldg(toff + vb + 1);
       // two-stage pipeline: the next chunk's dependent loads fly during this walk
@@ -490,22 +634,7 @@ __device__ __forceinline__ void fan_bp_body(const Launch &L, const int unit) {
       int c = b0 + warp * 32;
       uint4 e = (c + lane < b1) ? __ldg(S.run + c + lane) : kZ;
       uint4 h1 = __ldg(reinterpret_cast<const uint4 *>(S.rays + e.x) + 1);
-      auto load_r = [&](unsigned bin, float(&r)[G]) {
-        if constexpr (G == 1) {
-          r[0] = __ldg(sino + bin);
-        } else if constexpr (G == 2) {
-          const float2 v = __ldg(reinterpret_cast<const float2 *>(spack) + bin);
-          r[0] = v.x;
-          r[1] = v.y;
-        } else {
-          static_assert(G == 4, "members are read as one float, float2 or float4");
-          const float4 v = __ldg(spack + bin);
-          r[0] = v.x;
-          r[1] = v.y;
-          r[2] = v.z;
-          r[3] = v.w;
-        }
-      };
+      auto load_r = [&](unsigned bin, float(&r)[G]) { bp_load_r<G>(sino, spack, bin, r); };
       float r0[G];
       load_r(e.x, r0);
       for (; c < b1; c += blockDim.x) {
@@ -625,30 +754,36 @@ __device__ __forceinline__ void fan_bp_body(const Launch &L, const int unit) {
   }
 }
 
-__global__ void __launch_bounds__(256) fan_bp_kernel(const Launch L) { fan_bp_body<1, kBpCopies1>(L, blockIdx.x); }
+template <int M>
+__global__ void __launch_bounds__(256) fan_bp_kernel(const Launch L) { fan_bp_body<1, kBpCopies1, M>(L, blockIdx.x); }
+// queued (persistent) launches choose per CTA
 __global__ void __launch_bounds__(256) fan_bp_queue_kernel(const Launch L) {
-  persistent_loop(L, [&](int unit) { fan_bp_body<1, kBpCopies1>(L, unit); });
+  persistent_loop(L, [&](int unit) { fan_bp_body<1, kBpCopies1, 2>(L, unit); });
 }
 // four CTAs per SM (at most 64 registers; some setup state spills, and the
 // walk's latency is hidden better than at three CTAs with 80: two outer
 // iterations of four C2 slices 52.8 -> 51.3 ms)
-__global__ void __launch_bounds__(256, 4) fan_bp_group_kernel(const Launch L) {
-  fan_bp_body<kGroupMax, kBpCopiesG>(L, blockIdx.x);
+// table forms: three CTAs (85 registers for the loads of several views in flight)
+template <int M>
+__global__ void __launch_bounds__(256, M != 0 ? 3 : 4) fan_bp_group_kernel(const Launch L) {
+  fan_bp_body<kGroupMax, kBpCopiesG, M>(L, blockIdx.x);
 }
 __global__ void __launch_bounds__(256, 4) fan_bp_group_queue_kernel(const Launch L) {
-  persistent_loop(L, [&](int unit) { fan_bp_body<kGroupMax, kBpCopiesG>(L, unit); });
+  persistent_loop(L, [&](int unit) { fan_bp_body<kGroupMax, kBpCopiesG, 2>(L, unit); });
 }
 // in a batch with groups, the scans alone and the pairs
+template <int M>
 __device__ __forceinline__ void fan_bp_small_body(const Launch &L, int unit) {
   const ScanDev &S = L.scans[find_scan(L.prefix, L.nscans, unit)];
   if (S.nmem <= 1)
-    fan_bp_body<1, kBpCopiesG>(L, unit);
+    fan_bp_body<1, kBpCopiesG, M>(L, unit);
   else
-    fan_bp_body<2, kBpCopiesG>(L, unit);
+    fan_bp_body<2, kBpCopiesG, M>(L, unit);
 }
-__global__ void __launch_bounds__(256, 3) fan_bp_small_kernel(const Launch L) { fan_bp_small_body(L, blockIdx.x); }
+template <int M>
+__global__ void __launch_bounds__(256, 3) fan_bp_small_kernel(const Launch L) { fan_bp_small_body<M>(L, blockIdx.x); }
 __global__ void __launch_bounds__(256, 3) fan_bp_small_queue_kernel(const Launch L) {
-  persistent_loop(L, [&](int unit) { fan_bp_small_body(L, unit); });
+  persistent_loop(L, [&](int unit) { fan_bp_small_body<2>(L, unit); });
 }
 
 // ---------------------------------------------------------------------------
@@ -994,9 +1129,19 @@ int launch_bp_group(const Launch &L, const Launch &Lsino, const Launch &Lsmall, 
   La.queue = nullptr;
   sino_absmax_kernel<<<L.nscans * kBpMaxParts, 256, 0, st>>>(La);
   fp_pack_kernel<<<sino_nctas, 256, 0, st>>>(Lsino, 1);
-  static int resg = 0, ress = 0;
-  launch_maybe_queued(fan_bp_group_kernel, fan_bp_group_queue_kernel, resg, L, nctas, 256, st);
-  launch_maybe_queued(fan_bp_small_kernel, fan_bp_small_queue_kernel, ress, Lsmall, small_nctas, 256, st);
+  static int resg[3] = {0, 0, 0}, ress[3] = {0, 0, 0};
+  auto group = [&](auto kern, int m) {
+    launch_maybe_queued(kern, fan_bp_group_queue_kernel, resg[m], L, nctas, 256, st);
+  };
+  auto small = [&](auto kern, int m) {
+    launch_maybe_queued(kern, fan_bp_small_queue_kernel, ress[m], Lsmall, small_nctas, 256, st);
+  };
+  if (L.bp_table == 1) group(fan_bp_group_kernel<1>, 1);
+  else if (L.bp_table == 2) group(fan_bp_group_kernel<2>, 2);
+  else group(fan_bp_group_kernel<0>, 0);
+  if (Lsmall.bp_table == 1) small(fan_bp_small_kernel<1>, 1);
+  else if (Lsmall.bp_table == 2) small(fan_bp_small_kernel<2>, 2);
+  else small(fan_bp_small_kernel<0>, 0);
   return n + (nctas > 0) + (small_nctas > 0);
 }
 
@@ -1013,8 +1158,10 @@ cudaError_t launch_bp(const Launch &L, int kind, int nctas, cudaStream_t st, con
     Launch La = L;  // the max |r| pass: one CTA per part, never queued
     La.queue = nullptr;
     sino_absmax_kernel<<<(L.scans ? L.nscans : 1) * kBpMaxParts, 256, 0, st>>>(La);
-    static int res = 0;
-    launch_maybe_queued(fan_bp_kernel, fan_bp_queue_kernel, res, L, nctas, 256, st);
+    static int res[3] = {0, 0, 0};
+    if (L.bp_table == 1) launch_maybe_queued(fan_bp_kernel<1>, fan_bp_queue_kernel, res[1], L, nctas, 256, st);
+    else if (L.bp_table == 2) launch_maybe_queued(fan_bp_kernel<2>, fan_bp_queue_kernel, res[2], L, nctas, 256, st);
+    else launch_maybe_queued(fan_bp_kernel<0>, fan_bp_queue_kernel, res[0], L, nctas, 256, st);
   }
   return cudaGetLastError();
 }

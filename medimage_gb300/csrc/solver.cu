@@ -53,6 +53,10 @@ void fill_scan_plan(ScanDev &S, const Plan &p) {
   S.blk_off = p.blk_off_d;
   S.run = p.run_d;
   S.tile_off = p.tile_off_d;
+  S.pt_meta = p.pt_meta_d;
+  S.pt_w = p.pt_w_d;
+  S.pt_woff = p.pt_woff_d;
+  S.pt_use = p.pt_meta_d ? p.bp_table : 0;
   S.ntiles_y = p.ntiles_y;
   S.nvb = p.nvb;
   S.bp_term_bits = p.bp_term_bits;
@@ -288,6 +292,20 @@ int Batch::set(const ScanDev *scans, int n, int kind_, int rpt_, cudaStream_t st
     add(FAM_PIX, s, pix_ctas(scans[s]));
     add(FAM_SINO, s, (scans[s].nbins + 255) / 256);
   }
+  // pixel tables: one kernel form when every scan of a launch agrees, else a
+  // choice per CTA
+  auto table_mode = [&](int fam) {
+    int with = 0, without = 0;
+    for (int s = 0; s < n; s++) {
+      if (pref[fam * (n + 1) + s + 1] == pref[fam * (n + 1) + s]) continue;
+      const ScanDev &S = scans[s];
+      const bool t = (kind == AT_GEOM_FAN || kind == AT_GEOM_RAYS) && (S.pt_use & (S.nmem > 1 ? 2 : 1)) != 0;
+      (t ? with : without)++;
+    }
+    return with == 0 ? 0 : without == 0 ? 1 : 2;
+  };
+  bp_table_main = table_mode(FAM_BP);
+  bp_table_small = table_mode(FAM_BPS);
   fp_total = pref[FAM_FP * (n + 1) + n];
   pix_total = pref[FAM_PIX * (n + 1) + n];
   sino_total = pref[FAM_SINO * (n + 1) + n];
@@ -388,13 +406,18 @@ int Batch::enqueue_fp(const Launch &L, cudaStream_t st) {
 
 int Batch::enqueue_bp(const Launch &L, cudaStream_t st) {
   if (group > 1) {  // max |r|, interleave each group's sinograms, then one run walk per group
-    const Launch Ls = retarget(L, FAM_SINO), Lsm = retarget(L, FAM_BPS);
-    launches += launch_bp_group(L, Ls, Lsm, bp_total, sino_total, bps_total, st);
+    const Launch Ls = retarget(L, FAM_SINO);
+    Launch Lb = L, Lsm = retarget(L, FAM_BPS);
+    Lb.bp_table = bp_table_main;
+    Lsm.bp_table = bp_table_small;
+    launches += launch_bp_group(Lb, Ls, Lsm, bp_total, sino_total, bps_total, st);
     AT_CUDA_TRY(cudaGetLastError());
     return AT_OK;
   }
   const Launch Lp = retarget(L, FAM_PIX);  // the per-pixel finishing pass of the cone-beam back projector
-  AT_CUDA_TRY(launch_bp(L, kind, bp_total, st, &Lp, pix_total));
+  Launch Lb = L;
+  Lb.bp_table = bp_table_main;
+  AT_CUDA_TRY(launch_bp(Lb, kind, bp_total, st, &Lp, pix_total));
   // max |r| pass + back projection (cone beam: its chunks, folds and per-pixel finish)
   launches += kind == AT_GEOM_GOLDNC ? 1 : kind == AT_GEOM_CONE ? cone_bp_launches(cone_chunks) : 2;
   return AT_OK;

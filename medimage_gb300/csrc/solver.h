@@ -38,6 +38,10 @@ struct Batch {
   int fp_total = 0, pix_total = 0, sino_total = 0, bp_total = 0, fp1_total = 0, fp2_total = 0, bps_total = 0;
   int group = 1;            // largest group of scans sharing a plan (projected together)
   int cone_chunks = 1;      // cone beam: chunks of views of the batch's largest back projection
+  // fan back projection: Launch::bp_table of the main launch (groups of three
+  // or four, or every scan when nothing is grouped) and of the launch of pairs
+  // and scans alone
+  int bp_table_main = 0, bp_table_small = 0;
   // slab forward projector: used when every plan of the batch has slab tables
   // of one CTA shape; one TMA descriptor per scan (of its pack buffer, in its
   // group's form)

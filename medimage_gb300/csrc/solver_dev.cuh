@@ -94,6 +94,12 @@ struct ScanDev {
   const uint8_t *blk_off;  // per 128-ray block: a ray leaves the grid
   const uint4 *run;          // back-projection runs grouped by 16x16 tile
   const int32_t *tile_off;   // [tile * nvb + view block]
+  // the plan's pixel table (Plan::pt_*), and which launches gather from it
+  // instead of walking tile runs: bit0 single scans, bit1 groups
+  const uint32_t *pt_meta;
+  const float *pt_w;
+  const int64_t *pt_woff;
+  int pt_use;
   int ntiles_y, nvb, bp_term_bits;
   float pixel_mm;
   // goldnc plan
@@ -150,6 +156,8 @@ struct Launch {
   int chunks;                    // cone back projection: chunks of the launch's largest scan (host side)
   int group;                     // projector launches: largest group of scans sharing a plan
   int tr;                        // forward projection: the scans' pack buffers hold transposed inputs
+  int bp_table;                  // fan back projection: 0 walk tile runs, 1 gather from pixel tables,
+                                 // 2 each CTA as its scan's plan says (ScanDev::pt_use)
   // persistent launches (projectors of a batch): a grid sized to the resident
   // CTAs pulls work units (the CTA indices of the ordinary launch) from a
   // queue; order[i] is the i-th unit handed out (all units of the costlier

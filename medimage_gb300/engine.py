@@ -82,6 +82,9 @@ class _PlanStats(C.Structure):
         ("slab_rows", C.c_int32),
         ("slab_wbox", C.c_int32),
         ("slab_fallback_ctas", C.c_int32),
+        ("bp_table_use", C.c_int32),
+        ("bp_table_bytes", C.c_int64),
+        ("bp_table_weights", C.c_int64),
     ]
 
 
@@ -123,6 +126,7 @@ SIGNATURES = {
     "at_plan_create_fan_ex": ([C.POINTER(_FanGeom), C.c_int32, C.POINTER(C.c_void_p)], C.c_int),
     "at_plan_create_goldnc": ([C.POINTER(C.c_void_p)], C.c_int),
     "at_plan_set_forward_variant": ([C.c_void_p, C.c_int32, C.c_int32, C.c_int32], C.c_int),
+    "at_plan_set_back_variant": ([C.c_void_p, C.c_int32], C.c_int),
     "at_set_batch_launch_mode": ([C.c_int32], C.c_int),
     "at_rowaction_create": ([C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)], C.c_int),
     "at_rowaction_destroy": ([C.c_void_p], None),
@@ -436,6 +440,15 @@ class Plan:
         """Pin the forward projector: (0, 0, 0) the L1 walk, else the slab
         projector with that CTA shape and slab height (bitwise the same sums)."""
         _check("at_plan_set_forward_variant", lib().at_plan_set_forward_variant(self._h, views, rays, rows))
+        st = _PlanStats()
+        _check("at_plan_get_stats", lib().at_plan_get_stats(self._h, C.byref(st)))
+        self.stats = {k: getattr(st, k) for k, _ in _PlanStats._fields_}
+
+    def set_back_variant(self, use: int) -> None:
+        """Back projector of later batches: bit0 single scans, bit1 groups of
+        scans sharing the plan gather from the pixel table (built on first
+        use); a clear bit walks tile runs.  Bitwise the same sums."""
+        _check("at_plan_set_back_variant", lib().at_plan_set_back_variant(self._h, use))
         st = _PlanStats()
         _check("at_plan_get_stats", lib().at_plan_get_stats(self._h, C.byref(st)))
         self.stats = {k: getattr(st, k) for k, _ in _PlanStats._fields_}

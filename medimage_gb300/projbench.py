@@ -1,7 +1,7 @@
 """Time the forward and back projectors alone on one workload geometry.
 
     python -m medimage_gb300.projbench [--config c1|c2|c4] [--n N] [--reps N] [--which fp,bp] [--group G]
-                                       [--variant l1|views,rays,rows]
+                                       [--variant l1|views,rays,rows] [--bp runs|table]
 
 Prints one JSON line per projector: average launch time (CUDA events on the
 launching stream around each launch, L2 flushed before each unless --warm), algorithmic bytes per launch (forward 4 S + 4 R, back
@@ -34,6 +34,9 @@ def main() -> None:
     ap.add_argument("--variant", default="",
                     help="forward projector of 2D plans: 'l1', or views,rays,rows of the slab projector "
                          "(default: the autotuner's choice)")
+    ap.add_argument("--bp", default="", choices=["", "runs", "table"],
+                    help="back projector of 2D plans: walk tile runs, or gather from the pixel table "
+                         "(default: the plan's choice)")
     args = ap.parse_args()
     if args.config == "c4":
         spec = configs.c4(n=args.n, nz=args.n)
@@ -46,6 +49,8 @@ def main() -> None:
         if args.variant:
             plan.set_forward_variant(*([0, 0, 0] if args.variant == "l1" else
                                        [int(x) for x in args.variant.split(",")]))
+        if args.bp:
+            plan.set_back_variant(3 if args.bp == "table" else 0)
         img = phantom.ellipse_phantom(plan.n, seed=spec.seed, n_random=spec.n_random)
         names = ("fan_fp_kernel", "fan_bp_kernel")
     L = engine.lib()
@@ -101,7 +106,8 @@ def main() -> None:
                           "algorithmic_bytes": nbytes, "gbs": round(nbytes / (ms / 1e3) / 1e9, 1),
                           "segments": S, "rays": R, "pixels": P,
                           "variant": {k: plan.stats[k] for k in ("fp_rays_per_thread", "slab_views", "slab_rays",
-                                                                 "slab_rows", "slab_wbox", "slab_fallback_ctas")
+                                                                 "slab_rows", "slab_wbox", "slab_fallback_ctas",
+                                                                 "bp_table_use", "bp_table_bytes")
                                       if k in plan.stats}}))
     if pset is not None:
         pset.close()

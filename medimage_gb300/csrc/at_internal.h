@@ -186,6 +186,9 @@ void retire_slab_tables(Plan &p);  // moves p.slab to p.retired_slabs
 // pixels in one view) or the table would exceed max_bytes
 int build_pixel_table(Plan &p, int64_t max_bytes, cudaStream_t st);
 void free_pixel_table(Plan &p);
+// AT_ECUDA when a bounded wait of the slab projector ran out since the last
+// call (its CTAs' outputs are void); called after a synchronisation
+int check_wait_timeouts();
 
 }  // namespace medimg
 

@@ -371,6 +371,7 @@ int project_host(const Plan &p, bool forward, const float *h_in, float *h_out) {
   if (din) cudaFreeAsync(din, st);
   if (dout) cudaFreeAsync(dout, st);
   if ((e = cudaStreamSynchronize(st)) != cudaSuccess && !rc) rc = cuda_error(e, "projection");
+  if (!rc) rc = check_wait_timeouts();
   cudaStreamDestroy(st);
   return rc;
 }
@@ -417,7 +418,7 @@ AT_API int at_stream_destroy(void *stream) {
 }
 AT_API int at_stream_sync(void *stream) {
   AT_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
-  return AT_OK;
+  return check_wait_timeouts();
 }
 
 // ---------------------------------------------------------------- solver
@@ -530,7 +531,7 @@ AT_API int at_solver_get_host(at_solver *s, int32_t scan, float *h_f, float *h_v
   if (h_v)
     AT_CUDA_TRY(cudaMemcpyAsync(h_v, S.buf[B_V], sizeof(float) * S.npix, cudaMemcpyDeviceToHost, (cudaStream_t)stream));
   AT_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
-  return AT_OK;
+  return check_wait_timeouts();
 }
 
 AT_API int at_solver_set_fv_host(at_solver *s, int32_t scan, const float *h_f, const float *h_v, void *stream) {

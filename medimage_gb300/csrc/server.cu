@@ -360,7 +360,8 @@ AT_API int at_server_result_info(const at_server *srv, int64_t id, int32_t *iter
 
 AT_API int at_server_run(at_server *srv, double max_seconds) {
   if (!srv) return set_error(AT_EINVAL, "at_server_run: null argument");
-  return srv->s.run(max_seconds > 0 ? max_seconds : 1e30);
+  const int rc = srv->s.run(max_seconds > 0 ? max_seconds : 1e30);
+  return rc ? rc : check_wait_timeouts();
 }
 
 AT_API int at_server_result(at_server *srv, int64_t id, float *h_f, float *h_v, double *latency_s, double *wait_s) {

@@ -30,9 +30,11 @@
 #include <climits>
 #include <cstring>
 #include <mutex>
+#include <string>
 #include <vector>
 
 #include "epilogue.cuh"
+#include "mbar.cuh"
 #include "solver.h"
 
 namespace medimg {
@@ -40,36 +42,6 @@ namespace medimg {
 __device__ unsigned g_slab_timeouts;
 
 namespace {
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-               : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
-  unsigned ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-// polls until the phase completes; false after kWaitLimit polls (each poll
-// may itself suspend the thread for a while), i.e. seconds, not forever
-constexpr int kWaitLimit = 1 << 22;
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
-  for (int i = 0; i < kWaitLimit; i++)
-    if (mbar_try_wait(bar, parity)) return true;
-  return false;
-}
 
 __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int c0, int c1, uint64_t *bar) {
   asm volatile(
@@ -465,6 +437,19 @@ int slab_timeouts(unsigned *out) {
   AT_CUDA_TRY(cudaMemcpyFromSymbol(&v, g_slab_timeouts, sizeof(v)));
   if (v) AT_CUDA_TRY(cudaMemcpyToSymbol(g_slab_timeouts, &zero, sizeof(zero)));
   *out = v;
+  return AT_OK;
+}
+
+// Bounded waits of the slab projector that ran out since the last call:
+// AT_ECUDA then, as those CTAs left their outputs void.  Called after a
+// synchronisation.
+int check_wait_timeouts() {
+  unsigned n = 0;
+  const int rc = slab_timeouts(&n);
+  if (rc) return rc;
+  if (n)
+    return set_error(AT_ECUDA, "slab projector: shared-memory copies did not arrive within the wait limit (" +
+                                   std::to_string(n) + " CTAs); their results are void");
   return AT_OK;
 }
 

@@ -108,9 +108,10 @@ def test_table_refuses_what_does_not_fit(engine):
 def test_solver_with_mixed_launches(engine, oracle):
     """A batch of three plans: four scans of one (a group of four, from its
     table), a pair of another (table for groups only) and one scan of a
-    third (no table), so the pairs-and-singles launch chooses per CTA.  Equal
-    bit for bit to the same batch walking tile runs, over two runs of the
-    captured graph."""
+    third: without a table, so the launch of pairs and scans alone chooses
+    per CTA, then with its table for single scans too, so that launch
+    gathers throughout.  Equal bit for bit to the same batch walking tile
+    runs, over two runs of the captured graph."""
     G = engine.FanGeometry.covering
     ga, gb, gc = G(96, 2.0, 120, 160), G(64, 3.0, 90, 128), G(80, 2.4, 72, 100)
     pa, pb, pc = engine.Plan.fan(ga), engine.Plan.fan(gb), engine.Plan.fan(gc)
@@ -139,8 +140,11 @@ def test_solver_with_mixed_launches(engine, oracle):
     ref = solve()
     pa.set_back_variant(3)
     pb.set_back_variant(2)
-    got = solve()
-    for r_run, g_run in zip(ref, got):
-        for (fr, vr), (fg, vg) in zip(r_run, g_run):
-            np.testing.assert_array_equal(fg, fr)
-            np.testing.assert_array_equal(vg, vr)
+    got = [solve()]
+    pc.set_back_variant(1)
+    got.append(solve())
+    for g in got:
+        for r_run, g_run in zip(ref, g):
+            for (fr, vr), (fg, vg) in zip(r_run, g_run):
+                np.testing.assert_array_equal(fg, fr)
+                np.testing.assert_array_equal(vg, vr)

@@ -732,9 +732,7 @@ Plan::~Plan() {
   cudaFree(cone_trig_d);
   free_slab_tables(slab);
   for (auto &r : retired_slabs) free_slab_tables(r);
-  cudaFree(pt_meta_d);
-  cudaFree(pt_w_d);
-  cudaFree(pt_woff_d);
+  free_pixel_table(*this);
 }
 
 }  // namespace medimg

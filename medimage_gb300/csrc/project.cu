@@ -45,13 +45,55 @@ namespace medimg {
 // as it would be alone, so results do not depend on the grouping or on the
 // copy a warp reads.
 
+// The members' values of element p as one T (float, float2 or float4; zeros
+// for absent or finished members)
+template <typename T>
+__device__ __forceinline__ T pack_elem(const float *const (&src)[kGroupMax], int p) {
+  float v[kGroupMax];
+#pragma unroll
+  for (int m = 0; m < kGroupMax; m++) v[m] = src[m] ? __ldg(src[m] + p) : 0.f;
+  if constexpr (sizeof(T) == 4) return v[0];
+  else if constexpr (sizeof(T) == 8) return make_float2(v[0], v[1]);
+  else return make_float4(v[0], v[1], v[2], v[3]);
+}
+
+// Images of a scan (or a group) into its pack buffer, row-major and transposed,
+// 32 x 32 pixels at a time through shared memory so that both copies are
+// written in whole rows: tiles (local, local + ncta, ...) of the scan's CTAs.
+template <typename T>
+__device__ __forceinline__ void pack_image_tiles(const float *const (&src)[kGroupMax], int n, T *pk, int local,
+                                                 int ncta, float4 (*raw)[33]) {
+  T(*tile)[33] = reinterpret_cast<T(*)[33]>(raw);  // 32 x 33 elements of T
+  const int lane = threadIdx.x & 31, row = threadIdx.x >> 5;  // 8 rows of 32 threads
+  const int tiles_y = (n + 31) / 32;
+  const size_t npix = (size_t)n * n;
+  for (int t = local; t < tiles_y * tiles_y; t += ncta) {
+    const int x0 = (t / tiles_y) * 32, y0 = (t % tiles_y) * 32;
+    for (int r = row; r < 32; r += 8) {
+      const int x = x0 + r, y = y0 + lane;
+      if (x < n && y < n) {
+        const T v = pack_elem<T>(src, x * n + y);
+        pk[(size_t)x * n + y] = v;
+        tile[r][lane] = v;
+      }
+    }
+    __syncthreads();
+    for (int r = row; r < 32; r += 8) {
+      const int y = y0 + r, x = x0 + lane;
+      if (x < n && y < n) pk[npix + (size_t)y * n + x] = tile[lane][r];
+    }
+    __syncthreads();
+  }
+}
+
 // Interleaves each group's projector inputs into the lead's pack buffer, one
 // float2 per element for a pair, one float4 for three or four members, zeros
 // for absent or finished members; images twice, row-major and transposed
 // (the forward projector reads whichever puts a warp's neighbouring rays in
-// fewer sectors), and for a scan alone only its image transposed: images (bins = 0,
-// over the pixel-pass CTAs) before a grouped forward projection, sinograms
-// (bins = 1, over the sinogram-pass CTAs) before a grouped back projection.
+// fewer sectors), and for a scan alone only its image as floats, row-major and
+// transposed: images (bins = 0, over the pixel-pass CTAs) before a grouped
+// forward projection, sinograms (bins = 1, over the sinogram-pass CTAs) before
+// a grouped back projection.
 __global__ void __launch_bounds__(256) fp_pack_kernel(const Launch L, int bins) {
   const int scan = find_scan(L.prefix, L.nscans, blockIdx.x);
   const ScanDev &S = L.scans[scan];
@@ -66,31 +108,17 @@ __global__ void __launch_bounds__(256) fp_pack_kernel(const Launch L, int bins) 
   }
   if (!any) return;
   const int cta0 = __ldg(L.prefix + scan), ncta = __ldg(L.prefix + scan + 1) - cta0;
-  const int n = S.n, npix = n * n;
-  const int count = bins ? S.nbins : npix;
-  if (S.nmem == 1) {  // a scan alone: the image as floats, row-major then transposed
-    float *t = reinterpret_cast<float *>(S.pack);
-    for (int p = (blockIdx.x - cta0) * blockDim.x + threadIdx.x; p < npix; p += ncta * blockDim.x) {
-      const float v = src[0] ? __ldg(src[0] + p) : 0.f;
-      t[p] = v;
-      t[npix + (p % n) * n + p / n] = v;
-    }
+  const int local = blockIdx.x - cta0;
+  if (!bins) {
+    __shared__ float4 raw[32][33];
+    if (S.nmem == 1) pack_image_tiles<float>(src, S.n, reinterpret_cast<float *>(S.pack), local, ncta, raw);
+    else if (S.nmem == 2) pack_image_tiles<float2>(src, S.n, reinterpret_cast<float2 *>(S.pack), local, ncta, raw);
+    else pack_image_tiles<float4>(src, S.n, S.pack, local, ncta, raw);
     return;
   }
-  for (int p = (blockIdx.x - cta0) * blockDim.x + threadIdx.x; p < count; p += ncta * blockDim.x) {
-    float v[kGroupMax];
-#pragma unroll
-    for (int m = 0; m < kGroupMax; m++) v[m] = src[m] ? __ldg(src[m] + p) : 0.f;
-    // images: also transposed, after the row-major copy (see fan_fp_kernel)
-    const int pt = bins ? -1 : npix + (p % n) * n + p / n;
-    if (S.nmem == 2) {
-      float2 *pk = reinterpret_cast<float2 *>(S.pack);
-      pk[p] = make_float2(v[0], v[1]);
-      if (pt >= 0) pk[pt] = make_float2(v[0], v[1]);
-    } else {
-      S.pack[p] = make_float4(v[0], v[1], v[2], v[3]);
-      if (pt >= 0) S.pack[pt] = make_float4(v[0], v[1], v[2], v[3]);
-    }
+  for (int p = local * blockDim.x + threadIdx.x; p < S.nbins; p += ncta * blockDim.x) {
+    if (S.nmem == 2) reinterpret_cast<float2 *>(S.pack)[p] = pack_elem<float2>(src, p);
+    else S.pack[p] = pack_elem<float4>(src, p);
   }
 }
 

@@ -11,11 +11,13 @@
 // Forward: thread per ray (detector columns fastest, so a warp's rays are
 // neighbours and share voxels in L1/L2), FP32 products summed per 32 segments
 // and the partial sums Kahan-folded, then the fused epilogue of the 2D
-// projectors.  Back: thread per ray, each term w*r scaled to an integer (one
-// FFMA, magic-number rounding) and added into a 64-bit integer accumulator per
-// voxel; integer sums do not depend on order, so the result is deterministic
-// without float atomics.  A per-voxel pass converts, runs the epilogue and
-// leaves the accumulator zero.
+// projectors.  Back: thread per ray, in chunks of views, each term w*r scaled
+// to an integer (one FFMA, magic-number rounding) and added with a 32-bit
+// reduction into the chunk's accumulator, whose sums a fold pass moves into
+// exact 64-bit ones between chunks; integer sums do not depend on order, so
+// the result is deterministic without float atomics.  A per-voxel pass adds
+// the last chunk, converts, runs the epilogue and leaves both accumulators
+// zero.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -315,7 +317,7 @@ __device__ __forceinline__ void red_add(int *p, int v) {
 // One chunk of views (L.chunk; S.bp_vchunk views each), rays in band order,
 // a grid-stride loop over the chunk's rays.  Each term w*r is rounded to an
 // integer below 2^22 (one FFMA, magic-number rounding) and added with a 32-bit
-// atomic into the chunk's accumulator; the chunk is short enough that no
+// reduction (red_add) into the chunk's accumulator; the chunk is short enough that no
 // voxel's sum can leave 32 bits (cone_bp_views_per_chunk), and the fold pass
 // moves it into the exact 64-bit sum before the next chunk.  Integer sums do
 // not depend on order, so the result is deterministic, and bitwise the same
@@ -347,7 +349,7 @@ __global__ void __launch_bounds__(kConeThreads) cone_bp_kernel(const Launch L) {
     // a warp's rays are neighbouring detector columns of one view; they lie
     // side by side along the view's column direction (cos, sin) in (x, y).
     // Where that is closer to x, they add into the x-contiguous accumulator,
-    // so the lanes of one atomic instruction share sectors
+    // so the lanes of one reduction instruction share sectors
     const float2 cs = __ldg(S.cone_trig + (int)(ray / S.ndets));
     const bool xfast = fabsf(cs.x) > fabsf(cs.y);
     int *acc = xfast ? S.bp_acc32x : S.bp_acc32;

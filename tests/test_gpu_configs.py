@@ -26,6 +26,8 @@ the FP64-vs-perturbed-FP64 distance (and within 1e-4 while that distance is
 below 1e-6), its PSNR within 0.05 dB of the FP64 run's, and its exit branches
 identical.
 """
+import dataclasses
+
 import numpy as np
 import pytest
 
@@ -95,10 +97,15 @@ def check_projectors(engine, oracle, g, plan, n_sample=400, seed=0):
     assert np.linalg.norm(got - ref) <= FP_TOL * scale, (rel_l2(got, ref), np.linalg.norm(got - ref) / scale)
 
 
-def test_c1_reconstruction_matches_fp64(engine, oracle):
+@pytest.mark.parametrize("mode", [0, 1])
+def test_c1_reconstruction_matches_fp64(engine, oracle, mode):
+    """Exact mode (GoldenC's projection count) and linear mode (the CG's
+    sinograms updated by linearity, A(f + c p) = Af + c Ap: 12 forward
+    projections per outer iteration instead of 29) against the same FP64
+    solve of GoldenC's algorithm."""
     spec = configs.c1()
     ph, sino = spec_data(engine, oracle, spec)
-    prm = configs.params_for(spec)
+    prm = dataclasses.replace(configs.params_for(spec), mode=mode)
     plan = engine.Plan.fan(spec.geom)
     S = engine.Solver([plan], prm)
     S.set_sino(0, sino)

@@ -483,28 +483,42 @@ __device__ __forceinline__ void reduce_and_finalize_group(const ScanDev *const (
     last[m] = is_last;
   }
   __syncthreads();
+  // the members this CTA arrived last for (the same for every thread), all in
+  // one pass: each member's partials are summed in the same order as alone
+  unsigned lm = 0;
+#pragma unroll
+  for (int m = 0; m < G; m++) lm |= last[m] ? 1u << m : 0u;
+  if (!lm) return;
+  __threadfence();
+  double acc[G];
+#pragma unroll
+  for (int m = 0; m < G; m++) acc[m] = 0.0;
+#pragma unroll 4
+  for (int c = threadIdx.x; c < ncta; c += blockDim.x)
+#pragma unroll
+    for (int m = 0; m < G; m++)
+      if ((lm >> m) & 1u) acc[m] += __ldcg(M[m]->partials + c);
+  double w[G];
+#pragma unroll
+  for (int m = 0; m < G; m++) w[m] = warp_sum_d(acc[m]);
+  __syncthreads();  // red[][] is free again
+  if (lane == 0)
+#pragma unroll
+    for (int m = 0; m < G; m++) red[warp][m] = w[m];
+  __syncthreads();
+  // thread m finishes member m (static member indices keep M[] in registers)
 #pragma unroll
   for (int m = 0; m < G; m++) {
-    if (!last[m]) continue;  // the same for every thread of the CTA
-    __threadfence();
+    if (threadIdx.x != m || !((lm >> m) & 1u)) continue;
+    double a = 0;
+    for (int ww = 0; ww < nw; ww++) a += red[ww][m];
+    double tot[1] = {a};
     const ScanDev &S = *M[m];
-    double acc = 0.0;
-#pragma unroll 8
-    for (int c = threadIdx.x; c < ncta; c += blockDim.x) acc += __ldcg(S.partials + c);
-    const double w = warp_sum_d(acc);
-    __syncthreads();  // red[][] is free again
-    if (lane == 0) red[warp][0] = w;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double a = 0;
-      for (int ww = 0; ww < nw; ww++) a += red[ww][0];
-      double tot[1] = {a};
-      S.ctl->arrive = 0u;
-      finalize_stage(S, L, tot);
-      __threadfence();
-    }
-    __syncthreads();
+    S.ctl->arrive = 0u;
+    finalize_stage(S, L, tot);
+    __threadfence();
   }
+  __syncthreads();
 }
 
 __device__ __forceinline__ void atomic_max_nonneg(unsigned *addr, float x) {

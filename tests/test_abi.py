@@ -115,3 +115,36 @@ def test_driver_program_links(tmp_path):
     subprocess.run(["gcc", "-O2", "-std=c99", f"-I{INCLUDE}", os.path.join(ROOT, "tests", "goldnc_driver.c"),
                     f"-L{lib_dir}", "-lat_engine", f"-Wl,-rpath,{lib_dir}", "-lm", "-o", str(exe)], check=True)
     assert exe.exists()
+
+
+@pytest.mark.skipif(shutil.which("gcc") is None, reason="needs gcc")
+def test_struct_layouts_match_the_header(tmp_path):
+    """Every struct the Python bindings mirror with ctypes has the size and
+    field offsets the C header gives it (a C program compiled with gcc prints
+    them), so no field can drift between include/at_engine.h and engine.py."""
+    from medimage_gb300 import engine as E
+
+    structs = {
+        "at_fan_geometry": E._FanGeom,
+        "at_cone_geometry": E._ConeGeom,
+        "at_rowaction_params": E._RowActionParams,
+        "at_params": E._Params,
+        "at_plan_stats": E._PlanStats,
+        "at_server_config": E._ServerConfig,
+        "at_server_stats": E._ServerStats,
+    }
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "at_engine.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'printf("{cname} sizeof %zu\\n", sizeof({cname}));')
+        for field, _ in py._fields_:
+            lines.append(f'printf("{cname} {field} %zu\\n", offsetof({cname}, {field}));')
+    lines.append("return 0; }")
+    src, exe = tmp_path / "layout.c", tmp_path / "layout"
+    src.write_text("\n".join(lines) + "\n")
+    subprocess.run(["gcc", "-std=c11", "-I", INCLUDE, str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    got = {(a, b): int(c) for a, b, c in (line.split() for line in out if line.strip())}
+    for cname, py in structs.items():
+        assert got[(cname, "sizeof")] == C.sizeof(py), cname
+        for field, _ in py._fields_:
+            assert got[(cname, field)] == getattr(py, field).offset, (cname, field)

@@ -414,7 +414,8 @@ __global__ void __launch_bounds__(128) fan_fp_queue_kernel(const Launch L) {
 constexpr int kBpPitch = kBpTile + 1;  // padded row pitch of the accumulator
 constexpr int kBpAccWords = kBpTile * kBpPitch;
 constexpr int kBpCopies1 = 4;  // copies, single-scan launches (C2: 1 copy 0.33 ms, 4 copies 0.275 ms)
-constexpr int kBpCopiesG = 8;  // copies per member, grouped launches (four slices: 2 copies 0.90 ms, 4 0.785, 8 0.764)
+constexpr int kBpCopiesG = 8;  // copies per member, grouped launches (four slices: 2 copies 0.90 ms, 4 0.785, 8 0.764;
+                                // sixteen slices: 8 copies 2.52 ms, 4 copies at five or six CTAs per SM 2.70-2.72)
 template <int C>
 constexpr int bp_copy_stride() {
   return kBpAccWords + ((32 / C - kBpAccWords % 32) % 32 + 32) % 32;
